@@ -1,0 +1,146 @@
+/*
+ * warp_reactor.h -- C ABI of the GB300 primordial-chemistry grid integrator.
+ *
+ * The integrator advances N independent chemistry cells (14 species number
+ * densities + internal energy) through the free-fall collapse schedule of the
+ * reference reproducer under the "gridwide-independent" policy: every outer step a
+ * prepare kernel perturbs each cell and publishes its free-fall dt, the device
+ * takes the grid-wide minimum, and the advance kernel integrates every cell over
+ * that dt with its own ROS2S controller.
+ *
+ * Conventions
+ *  - Every entry point returns an int status with the reference's
+ *    IntegratorResult values (reproducer.cpp:30-37): WR_SUCCESS = 1 on success,
+ *    a negative code on failure.  Nothing throws across this boundary.
+ *  - The first failure recorded on the device wins (compare-and-swap from
+ *    WR_SUCCESS), as in reproducer.cpp:7716,7724,7782.  After a failure the cell
+ *    states may be partially committed, as in the reference.
+ *  - A context owns all device memory it allocates; host arrays belong to the
+ *    caller.  One context = one CUDA device and one stream; calls are synchronous
+ *    with respect to the host and must come from one host thread at a time.
+ *  - wr_collapse_state has the byte layout of the reference's CollapseState
+ *    (reproducer.cpp:7455-7461, 216 bytes), so a reference caller can pass
+ *    cells.data() of its std::vector<CollapseState> directly.
+ */
+#ifndef WARP_REACTOR_H
+#define WARP_REACTOR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WR_NUM_SPECIES 14
+#define WR_NEQS 15
+#define WR_MAX_COLLAPSE_STEPS 1000
+
+/* IntegratorResult codes, reproducer.cpp:30-37. */
+enum {
+    WR_SUCCESS = 1,
+    WR_BAD_INPUTS = -1,
+    WR_DT_UNDERFLOW = -2,
+    WR_TOO_MANY_STEPS = -4,
+    WR_TOO_MUCH_ACCURACY_REQUESTED = -5,
+    WR_LU_DECOMPOSITION_ERROR = -7
+};
+
+/* IntegratorStats, reproducer.cpp:7433-7441. */
+typedef struct wr_integrator_stats {
+    uint64_t internal_steps;
+    uint64_t rhs_calls;
+    uint64_t jacobian_calls;
+    uint64_t decompositions;
+    uint64_t linear_solves;
+    uint64_t accepted_steps;
+    uint64_t rejected_steps;
+} wr_integrator_stats;
+
+/* CollapseState (burn_t current; time; density_driver; completed_steps; stats),
+ * reproducer.cpp:263-268 and 7455-7461.  Species order: E, Hp, H, Hm, Dp, D, H2p,
+ * Dm, H2, HDp, HD, HEpp, HEp, HE (reproducer.cpp:228-229). */
+typedef struct wr_collapse_state {
+    double rho;
+    double T;
+    double e;
+    double xn[WR_NUM_SPECIES];
+    double time;
+    double density_driver;
+    int32_t completed_steps;
+    int32_t reserved_;
+    wr_integrator_stats stats;
+} wr_collapse_state;
+
+/* Packed 172-byte final-state record of final_states_grid<N>_<backend>.bin,
+ * reproducer.cpp:7488-7505 (little-endian, no padding). */
+#pragma pack(push, 1)
+typedef struct wr_packed_final_state {
+    int32_t cell, i, j, k, completed_steps;
+    double time, density_driver, rho, T, e;
+    double xn[WR_NUM_SPECIES];
+} wr_packed_final_state;
+#pragma pack(pop)
+
+/* Arithmetic used for exp/log/cbrt on the device.
+ *  WR_MATH_PORTABLE: the project's own bit-reproducible exp/log/cbrt (integer
+ *    fixed-point cores), identical on the GPU and in the CPU oracle.  Default.
+ *  WR_MATH_CUDA: CUDA's libm, the arithmetic of the reference's own CUDA build. */
+enum { WR_MATH_PORTABLE = 0, WR_MATH_CUDA = 1 };
+
+typedef struct wr_ctx wr_ctx;
+
+/* Create a context for num_cells cells on CUDA device `device`.  Allocates the
+ * structure-of-arrays cell state and the step scratch.  Replaces the allocation
+ * half of run_cells_cuda (reproducer.cpp:7794-7828). */
+int wr_create(int num_cells, int device, int math_mode, wr_ctx** out);
+
+/* Release every device buffer of the context (reproducer.cpp:7967-7973). */
+void wr_destroy(wr_ctx* ctx);
+
+/* Copy num_cells host records into the device state (AoS -> SoA transpose on the
+ * device) and reset the failure code.  reproducer.cpp:7822-7834. */
+int wr_upload(wr_ctx* ctx, const wr_collapse_state* cells);
+
+/* Copy the device state back into host records (SoA -> AoS).
+ * reproducer.cpp:7961-7966. */
+int wr_download(wr_ctx* ctx, wr_collapse_state* cells);
+
+/* One prepare launch plus the device grid minimum.  Replaces
+ * prepare_grid_timestep_kernel (reproducer.cpp:7696-7734) and the host scan of
+ * all candidates (reproducer.cpp:7865-7893).  *dt_grid_out receives the minimum
+ * candidate dt, or DBL_MAX when no cell is a candidate. */
+int wr_prepare(wr_ctx* ctx, int completed_global_steps, double grid_time, int step,
+               int perturb, double* dt_grid_out);
+
+/* One advance launch.  Replaces advance_collapse_gridwide_kernel
+ * (reproducer.cpp:7736-7785) and the counter read-back (:7903-7956).
+ * *integrated_out receives the number of cells that committed the step. */
+int wr_advance(wr_ctx* ctx, int completed_global_steps, double next_grid_time,
+               double dt_grid, int* integrated_out);
+
+/* The whole outer loop (reproducer.cpp:7856-7959) on the device state: up to
+ * WR_MAX_COLLAPSE_STEPS prepare/min/advance steps.  *completed_global_steps is read
+ * as the starting count and receives the final count. */
+int wr_run(wr_ctx* ctx, int perturb, int* completed_global_steps);
+
+/* Drop-in for run_cells_cuda (reproducer.cpp:7791-7975): create, upload, run,
+ * download, destroy, on the current CUDA device. */
+int wr_run_cells(wr_collapse_state* cells, int num_cells, int perturb,
+                 int* completed_global_steps);
+
+/* The reference's initial collapse cell (make_collapse_state,
+ * reproducer.cpp:7533-7546). */
+void wr_make_collapse_state(wr_collapse_state* out);
+
+/* Text of the last error recorded on this host thread ("" if none). */
+const char* wr_last_error(void);
+
+/* Number of kernels this library has launched since it was loaded. */
+uint64_t wr_kernel_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WARP_REACTOR_H */
