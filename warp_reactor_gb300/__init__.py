@@ -1,0 +1,201 @@
+"""warp_reactor_gb300 -- GB300-native primordial-chemistry grid integrator.
+
+Python host mirror of the reference reproducer's CUDA host path
+(reproducer.cpp:7791-7975, ``run_cells_cuda``) over the C ABI in
+``include/warp_reactor.h``.  The compute path is the CUDA library
+``_build/libwarp_reactor.so`` (sm_103a); there is no CPU fallback: every entry
+point raises if the library cannot be loaded.
+
+Names follow the reference: a *cell* is one independent chemistry state
+(``CollapseState``), ``completed_global_steps`` counts outer collapse steps, the
+grid is ``grid_dim**3`` cells.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libwarp_reactor.so")
+
+NUM_SPECIES = 14
+NEQS = 15
+MAX_COLLAPSE_STEPS = 1000
+SPECIES = ("E", "Hp", "H", "Hm", "Dp", "D", "H2p", "Dm", "H2", "HDp", "HD", "HEpp", "HEp", "HE")
+
+# IntegratorResult, reproducer.cpp:30-37
+SUCCESS = 1
+BAD_INPUTS = -1
+DT_UNDERFLOW = -2
+TOO_MANY_STEPS = -4
+TOO_MUCH_ACCURACY_REQUESTED = -5
+LU_DECOMPOSITION_ERROR = -7
+
+MATH_PORTABLE = 0
+MATH_CUDA = 1
+
+# CollapseState, reproducer.cpp:7455-7461 (216 bytes)
+STATS_FIELDS = ("internal_steps", "rhs_calls", "jacobian_calls", "decompositions",
+                "linear_solves", "accepted_steps", "rejected_steps")
+COLLAPSE_STATE = np.dtype([
+    ("rho", "<f8"), ("T", "<f8"), ("e", "<f8"), ("xn", "<f8", (NUM_SPECIES,)),
+    ("time", "<f8"), ("density_driver", "<f8"), ("completed_steps", "<i4"), ("reserved_", "<i4"),
+    ("stats", [(f, "<u8") for f in STATS_FIELDS]),
+])
+assert COLLAPSE_STATE.itemsize == 216
+
+# PackedFinalState, reproducer.cpp:7488-7505 (172 bytes, packed)
+PACKED_FINAL_STATE = np.dtype([
+    ("cell", "<i4"), ("i", "<i4"), ("j", "<i4"), ("k", "<i4"), ("completed_steps", "<i4"),
+    ("time", "<f8"), ("density_driver", "<f8"), ("rho", "<f8"), ("T", "<f8"), ("e", "<f8"),
+    ("xn", "<f8", (NUM_SPECIES,)),
+])
+assert PACKED_FINAL_STATE.itemsize == 172
+
+
+class WarpReactorError(RuntimeError):
+    def __init__(self, code: int, what: str):
+        super().__init__(f"{what} failed with IntegratorResult {code}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run warp_reactor_gb300.build.build_all() "
+                               "(the integrator has no CPU fallback)")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, ip, dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)
+        L.wr_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]
+        L.wr_destroy.argtypes = [vp]
+        L.wr_destroy.restype = None
+        L.wr_upload.argtypes = [vp, vp]
+        L.wr_download.argtypes = [vp, vp]
+        L.wr_prepare.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, dp]
+        L.wr_advance.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ip]
+        L.wr_run.argtypes = [vp, ctypes.c_int, ip]
+        L.wr_run_cells.argtypes = [vp, ctypes.c_int, ctypes.c_int, ip]
+        L.wr_make_collapse_state.argtypes = [vp]
+        L.wr_make_collapse_state.restype = None
+        L.wr_last_error.restype = ctypes.c_char_p
+        L.wr_kernel_launch_count.restype = ctypes.c_uint64
+        _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    return lib().wr_last_error().decode()
+
+
+def kernel_launch_count() -> int:
+    return int(lib().wr_kernel_launch_count())
+
+
+def make_collapse_state() -> np.ndarray:
+    """The reference's initial cell, ``make_collapse_state`` (reproducer.cpp:7543-7546)."""
+    out = np.zeros(1, COLLAPSE_STATE)
+    lib().wr_make_collapse_state(out.ctypes.data)
+    return out[0]
+
+
+def make_grid(grid_dim: int) -> np.ndarray:
+    n = int(grid_dim) ** 3
+    cells = np.empty(n, COLLAPSE_STATE)
+    cells[:] = make_collapse_state()
+    return cells
+
+
+class Context:
+    """Device state for ``num_cells`` cells on one GPU (``wr_create`` .. ``wr_destroy``)."""
+
+    def __init__(self, num_cells: int, device: int = 0, math: int = MATH_PORTABLE):
+        h = ctypes.c_void_p()
+        rc = lib().wr_create(int(num_cells), int(device), int(math), ctypes.byref(h))
+        if rc != SUCCESS:
+            raise WarpReactorError(rc, f"wr_create ({last_error()})")
+        self.handle = h
+        self.num_cells = int(num_cells)
+
+    def close(self):
+        if self.handle:
+            lib().wr_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check_cells(self, cells):
+        if cells.dtype != COLLAPSE_STATE or cells.shape != (self.num_cells,) or not cells.flags.c_contiguous:
+            raise ValueError("cells must be a contiguous COLLAPSE_STATE array of num_cells records")
+
+    def upload(self, cells: np.ndarray) -> None:
+        self._check_cells(cells)
+        rc = lib().wr_upload(self.handle, cells.ctypes.data)
+        if rc != SUCCESS:
+            raise WarpReactorError(rc, f"wr_upload ({last_error()})")
+
+    def download(self, cells: np.ndarray) -> None:
+        self._check_cells(cells)
+        rc = lib().wr_download(self.handle, cells.ctypes.data)
+        if rc != SUCCESS:
+            raise WarpReactorError(rc, f"wr_download ({last_error()})")
+
+    def prepare(self, completed_global_steps: int, grid_time: float, step: int, perturb: bool):
+        """prepare_grid_timestep_kernel + grid minimum -> (result, dt_grid)."""
+        dt = ctypes.c_double()
+        rc = lib().wr_prepare(self.handle, completed_global_steps, grid_time, step, int(bool(perturb)),
+                              ctypes.byref(dt))
+        return rc, dt.value
+
+    def advance(self, completed_global_steps: int, next_grid_time: float, dt_grid: float):
+        """advance_collapse_gridwide_kernel -> (result, integrated_count)."""
+        cnt = ctypes.c_int()
+        rc = lib().wr_advance(self.handle, completed_global_steps, next_grid_time, dt_grid, ctypes.byref(cnt))
+        return rc, cnt.value
+
+    def run(self, perturb: bool = True, completed_global_steps: int = 0):
+        """The whole outer loop on the device -> (result, completed_global_steps)."""
+        cgs = ctypes.c_int(completed_global_steps)
+        rc = lib().wr_run(self.handle, int(bool(perturb)), ctypes.byref(cgs))
+        return rc, cgs.value
+
+
+def run_cells(cells: np.ndarray, perturb: bool = True, math: int = MATH_PORTABLE, device: int = 0):
+    """Mirror of ``run_cells_cuda(cells, perturb, completed_global_steps)``: advances
+    ``cells`` in place and returns (IntegratorResult, completed_global_steps)."""
+    with Context(len(cells), device, math) as ctx:
+        ctx.upload(cells)
+        rc, cgs = ctx.run(perturb)
+        ctx.download(cells)
+    return rc, cgs
+
+
+def pack_final_states(cells: np.ndarray, grid_dim: int) -> np.ndarray:
+    """``make_packed_final_state`` for every cell (reproducer.cpp:8289-8305)."""
+    n = len(cells)
+    out = np.zeros(n, PACKED_FINAL_STATE)
+    idx = np.arange(n, dtype=np.int64)
+    out["cell"] = idx
+    out["i"] = idx % grid_dim
+    out["j"] = (idx // grid_dim) % grid_dim
+    out["k"] = idx // (grid_dim * grid_dim)
+    out["completed_steps"] = cells["completed_steps"]
+    for f in ("time", "density_driver", "rho", "T", "e", "xn"):
+        out[f] = cells[f]
+    return out

@@ -1,0 +1,533 @@
+// wr_kernels.cuh -- device kernels of the gridwide-independent integrator.
+//
+// Data layout in HBM (structure of arrays, one slot per cell, coalesced):
+//   rho[N] T[N] e[N] xn[14][N] time[N] driver[N] steps[N] stats[7][N]
+// Step control lives in one small device struct (StepCtl) so that a whole outer
+// step -- prepare, grid minimum, advance, commit -- runs without a host round
+// trip and can be captured in a CUDA graph.
+//
+// Kernels (reference counterparts in reproducer.cpp):
+//   k_unpack / k_pack      AoS host records <-> SoA device state (H2D/D2H at
+//                          :7822-7828, :7961-7966)
+//   k_prepare              prepare_grid_timestep_kernel (:7696-7734) fused with
+//                          the grid minimum (host scan at :7888-7893): each block
+//                          reduces its candidates and does one 64-bit atomicMin on
+//                          the bit pattern of a positive double (monotone in value)
+//   k_decide               the host checks between the two kernels (:7888-7909)
+//   k_advance              advance_collapse_gridwide_kernel (:7736-7785) as a
+//                          persistent kernel: every lane owns one cell at a time,
+//                          runs the ROS2S controller of RODAS::integrate
+//                          (:7205-7347) one attempt per loop trip, and takes the
+//                          next cell from a device work queue as soon as its cell
+//                          is done, so lanes of a warp stay busy although cells
+//                          need 1 to 10+ attempts per step
+//   k_finalize             the host bookkeeping after the advance (:7930-7958)
+#pragma once
+
+#include <cfloat>
+#include <stdint.h>
+
+#include "../../include/warp_reactor.h"
+#include "wr_physics.cuh"
+
+#ifndef WR_NET_HD
+#define WR_NET_HD __device__ __forceinline__
+#endif
+#include "generated/network_gen.h"
+
+namespace wr {
+
+struct DevState {
+    double* rho;
+    double* T;
+    double* e;
+    double* xn;      // [14][n]
+    double* time;
+    double* driver;
+    int* steps;
+    uint64_t* stats;  // [7][n]
+    int n;
+};
+
+struct StepCtl {
+    unsigned long long dmin_bits;  // grid minimum of the candidates (double bits)
+    int failure;                   // first failure, WR_SUCCESS otherwise
+    int integrated;                // cells committed by the last advance
+    int stop;                      // 1 once the outer loop has ended
+    int cgs;                       // completed global steps
+    int step;                      // outer-loop index (perturbation seed)
+    int perturb;
+    double grid_time;
+    double dt_grid;
+    double next_grid_time;
+    unsigned int queue;            // work-queue head of k_advance
+    unsigned int pad_;
+};
+
+constexpr unsigned long long kDblMaxBits = 0x7fefffffffffffffULL;
+
+// ------------------------------------------------------------------ math policies
+struct PortableMath {
+    static __device__ __forceinline__ double exp(double x) { return wr_exp(x); }
+    static __device__ __forceinline__ double log(double x) { return wr_log(x); }
+    static __device__ __forceinline__ double cbrt(double x) { return wr_cbrt(x); }
+    static __device__ __forceinline__ double sqrt(double x) { return ::sqrt(x); }
+    static __device__ __forceinline__ double fabs(double x) { return ::fabs(x); }
+    static __device__ __forceinline__ double div(double a, double b) { return a / b; }
+};
+
+struct CudaMath {
+    static __device__ __forceinline__ double exp(double x) { return ::exp(x); }
+    static __device__ __forceinline__ double log(double x) { return ::log(x); }
+    static __device__ __forceinline__ double cbrt(double x) { return ::cbrt(x); }
+    static __device__ __forceinline__ double sqrt(double x) { return ::sqrt(x); }
+    static __device__ __forceinline__ double fabs(double x) { return ::fabs(x); }
+    static __device__ __forceinline__ double div(double a, double b) { return a / b; }
+};
+
+// Out-of-line transcendentals: the generated network makes several hundred
+// exp/log calls per evaluation; one shared copy keeps the kernel's instruction
+// footprint small.
+static __device__ __noinline__ double wr_exp_call(double x) { return wr_exp(x); }
+static __device__ __noinline__ double wr_log_call(double x) { return wr_log(x); }
+struct PortableMathCall {
+    static __device__ __forceinline__ double exp(double x) { return wr_exp_call(x); }
+    static __device__ __forceinline__ double log(double x) { return wr_log_call(x); }
+    static __device__ __forceinline__ double cbrt(double x) { return wr_cbrt(x); }
+    static __device__ __forceinline__ double sqrt(double x) { return ::sqrt(x); }
+    static __device__ __forceinline__ double fabs(double x) { return ::fabs(x); }
+    static __device__ __forceinline__ double div(double a, double b) { return a / b; }
+};
+
+
+// ------------------------------------------------------------------ prepare
+__device__ __forceinline__ void record_failure(StepCtl* ctl, int code) {
+    atomicCAS(&ctl->failure, WR_SUCCESS, code);
+}
+
+template <int B>
+__global__ void __launch_bounds__(B) k_prepare(DevState s, StepCtl* ctl) {
+    __shared__ unsigned long long red[B / 32];
+    const int stop = ctl->stop;
+    const int cgs = ctl->cgs;
+    const double grid_time = ctl->grid_time;
+    const int step = ctl->step;
+    const bool perturb = ctl->perturb != 0;
+    const int failure0 = ctl->failure;
+    const int cell = blockIdx.x * B + threadIdx.x;
+    unsigned long long cand = kDblMaxBits;
+    if (!stop && failure0 == WR_SUCCESS && cell < s.n) {
+        const int n = s.n;
+        const int cs = s.steps[cell];
+        if (cs >= cgs) {
+            if (cs != cgs || s.time[cell] != grid_time) {
+                record_failure(ctl, WR_BAD_INPUTS);
+            } else {
+                double xn[NS];
+#pragma unroll
+                for (int k = 0; k < NS; ++k) xn[k] = s.xn[k * n + cell];
+                double driver = s.driver[cell];
+                // apply_perturbation, reproducer.cpp:7564-7580
+                if (perturb && step != 0 && step % kPerturbInterval == 0) {
+                    const double factor = perturbation_factor(cell, step);
+                    driver *= factor;
+                    const double rho = s.rho[cell] * factor;
+#pragma unroll
+                    for (int k = 0; k < NS; ++k) xn[k] *= factor;
+                    renormalize(xn, rho);
+                    const double T = eos_T_from_e(xn, s.e[cell]);
+                    s.rho[cell] = rho;
+                    s.T[cell] = T;
+#pragma unroll
+                    for (int k = 0; k < NS; ++k) s.xn[k * n + cell] = xn[k];
+                }
+                const double dt = collapse_timestep(xn);
+                if (!valid_positive(dt) || !valid_positive(driver)) {
+                    record_failure(ctl, WR_BAD_INPUTS);
+                } else if (dt < 10.0) {
+                    const double tff = dt / kTffReduc;
+                    driver += dt * (driver / tff);
+                } else {
+                    cand = static_cast<unsigned long long>(__double_as_longlong(dt));
+                }
+                s.driver[cell] = driver;
+            }
+        }
+    }
+    // block minimum of positive-double bit patterns, then one atomic per block
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(0xffffffffu, cand, off);
+        cand = o < cand ? o : cand;
+    }
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = cand;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long m = red[0];
+#pragma unroll
+        for (int w = 1; w < B / 32; ++w) m = red[w] < m ? red[w] : m;
+        if (m != kDblMaxBits) atomicMin(&ctl->dmin_bits, m);
+    }
+}
+
+
+// ------------------------------------------------------------------ advance
+// Per-lane matrix storage in shared memory: element (r, c) of lane l at
+// smem[(r*15 + c) * B + l]; 32 consecutive lanes touch 32 consecutive doubles.
+template <int B>
+struct Mat {
+    double* base;
+    __device__ __forceinline__ double& operator()(int r, int c) const { return base[(r * NEQ + c) * B]; }
+};
+
+// J sink of the generated network: E = -J into shared memory, J into the lane's
+// global backup (re-read only when an attempt is retried with the same J)
+template <int B>
+struct JSink {
+    Mat<B> E;
+    double* jb;
+    int stride;
+    __device__ __forceinline__ void operator()(int r, int c, double v) {
+        E(r, c) = -v;
+        jb[(r * NEQ + c) * stride] = v;
+    }
+};
+
+// burn_state_from_y (reproducer.cpp:7029-7038): floored X and T from y
+__device__ __forceinline__ void state_from_y(const double* y, double* X, double& T) {
+#pragma unroll
+    for (int k = 0; k < NS; ++k) X[k] = smax(y[k], kFloor);
+    T = eos_T_from_e(X, y[NS]);
+}
+
+// lu_decomposition<15> (reproducer.cpp:96-151) on the lane's shared-memory matrix.
+// Row interchanges move whole rows; pivot indices are returned in ip.
+template <int B>
+__device__ __forceinline__ int lu_decompose(Mat<B> A, int* ip) {
+    int info = 0;
+#pragma unroll
+    for (int k = 0; k < NEQ - 1; ++k) {
+        int p = k;
+        double maxv = ::fabs(A(k, k));
+#pragma unroll
+        for (int i = k + 1; i < NEQ; ++i) {
+            const double v = ::fabs(A(i, k));
+            if (v > maxv) {
+                maxv = v;
+                p = i;
+            }
+        }
+        ip[k] = p;
+        const double apk = A.base[(p * NEQ + k) * B];
+        if (apk != 0.0) {
+            if (p != k) {
+                A.base[(p * NEQ + k) * B] = A(k, k);
+                A(k, k) = apk;
+#pragma unroll
+                for (int j = k + 1; j < NEQ; ++j) {
+                    const double tr = A.base[(p * NEQ + j) * B];
+                    A.base[(p * NEQ + j) * B] = A(k, j);
+                    A(k, j) = tr;
+                }
+            }
+            const double mult = -1.0 / A(k, k);
+            double l[NEQ];
+#pragma unroll
+            for (int i = k + 1; i < NEQ; ++i) {
+                l[i] = A(i, k) * mult;
+                A(i, k) = l[i];
+            }
+#pragma unroll
+            for (int j = k + 1; j < NEQ; ++j) {
+                const double t = A(k, j);
+#pragma unroll
+                for (int i = k + 1; i < NEQ; ++i) A(i, j) = A(i, j) + t * l[i];
+            }
+        } else {
+            info = k + 1;
+        }
+    }
+    ip[NEQ - 1] = NEQ - 1;
+    if (A(NEQ - 1, NEQ - 1) == 0.0) info = NEQ;
+    return info;
+}
+
+// lu_solve<15> (reproducer.cpp:154-181); x stays in registers, the pivot swap is a
+// select chain instead of a dynamically indexed register array
+template <int B>
+__device__ __forceinline__ void lu_solve(Mat<B> LU, const int* ip, double* x) {
+#pragma unroll
+    for (int k = 0; k < NEQ - 1; ++k) {
+        const int p = ip[k];
+        double t = x[k];
+#pragma unroll
+        for (int i = k + 1; i < NEQ; ++i) t = (p == i) ? x[i] : t;
+        if (p != k) {
+#pragma unroll
+            for (int i = k + 1; i < NEQ; ++i) x[i] = (p == i) ? x[k] : x[i];
+            x[k] = t;
+        }
+#pragma unroll
+        for (int j = k + 1; j < NEQ; ++j) x[j] = x[j] + t * LU(j, k);
+    }
+#pragma unroll
+    for (int kb = 0; kb < NEQ; ++kb) {
+        const int k = NEQ - 1 - kb;
+        x[k] = x[k] / LU(k, k);
+        const double t = -x[k];
+#pragma unroll
+        for (int j = 0; j < k; ++j) x[j] = x[j] + t * LU(j, k);
+    }
+}
+
+struct Lane {
+    // ROS2S controller state of RODAS::integrate (reproducer.cpp:7225-7235)
+    double x, h, hacc, erracc, hopt, tout;
+    int n_step, n_accept, n_reject, n_jac, n_decomp, nsing;
+    bool reject, last, fresh;
+};
+
+template <class M, int B>
+__global__ void __launch_bounds__(B, 1) k_advance(DevState s, StepCtl* ctl, double* __restrict__ jbackup) {
+    extern __shared__ double smem[];
+    if (ctl->stop) return;
+    const int n = s.n;
+    const int cgs = ctl->cgs;
+    const double dt_grid = ctl->dt_grid;
+    const double next_grid_time = ctl->next_grid_time;
+    const int lane_slot = blockIdx.x * B + threadIdx.x;
+    const int nslots = gridDim.x * B;
+    Mat<B> E{smem + threadIdx.x};
+    double* jb = jbackup + lane_slot;
+
+    Lane L;
+    int cell = -1;
+    bool alive = true;   // lane may still take cells
+    bool have = false;   // lane holds a cell
+    double y[NEQ], f0[NEQ];
+    int ip[NEQ];
+    int integrated = 0;
+
+    while (__any_sync(0xffffffffu, alive)) {
+        // ---- bring the lane to "ready for an attempt"
+        while (alive) {
+            if (!have) {
+                if (ctl->failure != WR_SUCCESS) { alive = false; break; }
+                cell = static_cast<int>(atomicAdd(&ctl->queue, 1u));
+                if (cell >= n) { alive = false; break; }
+                // advance_collapse_gridwide_kernel prologue, reproducer.cpp:7748-7768
+                if (s.steps[cell] != cgs) continue;
+                double xn[NS];
+#pragma unroll
+                for (int k = 0; k < NS; ++k) xn[k] = s.xn[k * n + cell];
+                const double local_dt = collapse_timestep(xn);
+                if (local_dt < 10.0) continue;
+                const double old_density = s.driver[cell];
+                const double tff = local_dt / kTffReduc;
+                const double driver = old_density + dt_grid * (old_density / tff);
+                s.driver[cell] = driver;
+                if (!valid_positive(driver) || driver > kDriverLimit) continue;
+                const double ratio = driver / old_density;
+#pragma unroll
+                for (int k = 0; k < NS; ++k) xn[k] *= ratio;
+                const double rho = s.rho[cell] * ratio;
+                // burn_ros2s prologue (reproducer.cpp:7594-7606): e from T
+                const double e = eos_e_from_T(xn, s.T[cell]);
+                // the scaled pre-burn state is what a failed burn leaves behind
+                s.rho[cell] = rho;
+                s.e[cell] = e;
+#pragma unroll
+                for (int k = 0; k < NS; ++k) {
+                    s.xn[k * n + cell] = xn[k];
+                    y[k] = xn[k];
+                }
+                y[NS] = e;
+                // RODAS::integrate prologue, reproducer.cpp:7218-7235
+                L.tout = dt_grid;
+                L.x = 0.0;
+                double h0 = dt_grid;
+                if (::fabs(h0) <= 10.0 * kUround) h0 = 1.e-6;
+                L.h = smin(::fabs(h0), dt_grid);
+                L.reject = false;
+                L.last = false;
+                L.nsing = 0;
+                L.hacc = 0.0;
+                L.erracc = 1.0;
+                L.hopt = L.h;
+                L.n_step = 0;
+                L.n_accept = 0;
+                L.n_reject = 0;
+                L.n_jac = 0;
+                L.n_decomp = 0;
+                L.fresh = true;
+                have = true;
+            }
+            if (!L.fresh) break;
+            // outer-loop checks, reproducer.cpp:7236-7255
+            int code = 0;
+            if (L.n_step > kMaxSteps) code = WR_TOO_MANY_STEPS;
+            else if (0.1 * ::fabs(L.h) <= ::fabs(L.x) * kUround) code = WR_DT_UNDERFLOW;
+            else if (L.last) code = WR_SUCCESS;
+            if (code != 0) {
+                // burn_ros2s epilogue: counters, then commit or failure
+                const uint64_t st[7] = {
+                    static_cast<uint64_t>(L.n_step), static_cast<uint64_t>(3 * L.n_step),
+                    static_cast<uint64_t>(L.n_jac), static_cast<uint64_t>(L.n_decomp),
+                    static_cast<uint64_t>(3 * L.n_step), static_cast<uint64_t>(L.n_accept),
+                    static_cast<uint64_t>(L.n_reject)};
+#pragma unroll
+                for (int k = 0; k < 7; ++k) s.stats[k * n + cell] += st[k];
+                if (code == WR_SUCCESS) {
+                    double xn[NS];
+#pragma unroll
+                    for (int k = 0; k < NS; ++k) xn[k] = y[k];
+                    const double rho = s.rho[cell];
+                    renormalize(xn, rho);
+                    s.T[cell] = eos_T_from_e(xn, y[NS]);
+                    s.e[cell] = y[NS];
+#pragma unroll
+                    for (int k = 0; k < NS; ++k) s.xn[k * n + cell] = xn[k];
+                    s.time[cell] = next_grid_time;
+                    s.steps[cell] = cgs + 1;
+                    integrated += 1;
+                } else {
+                    record_failure(ctl, code);
+                }
+                have = false;
+                continue;
+            }
+            L.hopt = L.h;
+            if (L.x + L.h * 1.0001 >= L.tout) {
+                L.h = L.tout - L.x;
+                L.last = true;
+            }
+            break;
+        }
+        // ---- fresh outer iteration: Jacobian (fused with f(y))
+        if (alive && have && L.fresh) {
+            double X[NS], T;
+            state_from_y(y, X, T);
+            JSink<B> sink{E, jb, nslots};
+            wr_net_jac_rhs<M>(X, T, f0, sink);
+            L.n_jac += 1;
+            L.fresh = false;
+        } else if (alive && have) {
+            // retry with the same Jacobian: rebuild E = -J
+#pragma unroll
+            for (int r = 0; r < NEQ; ++r)
+#pragma unroll
+                for (int c = 0; c < NEQ; ++c) E(r, c) = -jb[(r * NEQ + c) * nslots];
+        }
+        // ---- one attempt of the inner loop, reproducer.cpp:7259-7345
+        if (alive && have) {
+            const double h = L.h;
+            const double fac = 1.0 / (h * kGamma);
+#pragma unroll
+            for (int i = 0; i < NEQ; ++i) E(i, i) = E(i, i) + fac;
+            const int info = lu_decompose<B>(E, ip);
+            if (info != 0) {
+                L.nsing += 1;
+                if (L.nsing >= 5) {
+                    // fails like the outer checks: counters then the failure code
+                    const uint64_t st[7] = {
+                        static_cast<uint64_t>(L.n_step), static_cast<uint64_t>(3 * L.n_step),
+                        static_cast<uint64_t>(L.n_jac), static_cast<uint64_t>(L.n_decomp),
+                        static_cast<uint64_t>(3 * L.n_step), static_cast<uint64_t>(L.n_accept),
+                        static_cast<uint64_t>(L.n_reject)};
+#pragma unroll
+                    for (int k = 0; k < 7; ++k) s.stats[k * n + cell] += st[k];
+                    record_failure(ctl, WR_LU_DECOMPOSITION_ERROR);
+                    have = false;
+                } else {
+                    L.h = h * 0.5;
+                    L.reject = true;
+                    L.last = false;
+                }
+            } else {
+                L.n_decomp += 1;
+                double ak1[NEQ], ak2[NEQ], w[NEQ];
+#pragma unroll
+                for (int i = 0; i < NEQ; ++i) ak1[i] = f0[i];
+                lu_solve<B>(E, ip, ak1);
+                // stages 2 and 3 share one inlined RHS evaluation
+#pragma unroll 1
+                for (int stage = 2; stage <= 3; ++stage) {
+                    double yn[NEQ];
+                    if (stage == 2) {
+#pragma unroll
+                        for (int i = 0; i < NEQ; ++i) {
+                            yn[i] = y[i] + kA21 * ak1[i];
+                            w[i] = (kC21 / h) * ak1[i];
+                        }
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < NEQ; ++i) {
+                            yn[i] = y[i] + kA31 * ak1[i] + kA32 * ak2[i];
+                            w[i] = (kC31 * ak1[i] + kC32 * ak2[i]) / h;
+                        }
+                    }
+                    double X[NS], T, dy[NEQ];
+                    state_from_y(yn, X, T);
+                    wr_net_rhs<M>(X, T, dy);
+#pragma unroll
+                    for (int i = 0; i < NEQ; ++i) w[i] += dy[i];
+                    lu_solve<B>(E, ip, w);
+                    if (stage == 2) {
+#pragma unroll
+                        for (int i = 0; i < NEQ; ++i) ak2[i] = w[i];
+                    }
+                }
+                // w = k3; candidate and error estimate, reproducer.cpp:7299-7304
+                double ynew[NEQ];
+                double err = 0.0;
+#pragma unroll
+                for (int i = 0; i < NEQ; ++i) {
+                    const double ak3 = w[i];
+                    ynew[i] = y[i] + kB1 * ak1[i] + kB2 * ak2[i] + ak3;
+                    const double wi = kE1 * ak1[i] + kE2 * ak2[i] + kE3 * ak3;
+                    const double rtol = i < NS ? kRtolSpec : kRtolEnergy;
+                    const double atol = i < NS ? kAtolSpec : kAtolEnergy;
+                    const double sk = atol + rtol * smax(::fabs(y[i]), ::fabs(ynew[i]));
+                    const double term = wi / sk;
+                    err += term * term;
+                }
+                err = ::sqrt(err / 15.0);
+                L.n_step += 1;
+                // step-size controller, reproducer.cpp:7308-7344
+                const double raw_fac = M::cbrt(err) / kSafe;
+                const double fac_step = smax(1.0 / kFacMax, smin(1.0 / kFacMin, raw_fac));
+                double hnew = h / fac_step;
+                if (err <= 1.0) {
+                    L.n_accept += 1;
+                    if (L.n_accept > 1) {
+                        const double facgus = smax(1.0 / kFacMax,
+                            smin(1.0 / kFacMin, (L.hacc / h) * M::cbrt((err * err) / L.erracc) / kSafe));
+                        hnew = h / smax(fac_step, facgus);
+                    }
+                    L.hacc = h;
+                    L.erracc = smax(1.e-2, err);
+#pragma unroll
+                    for (int i = 0; i < NEQ; ++i) y[i] = ynew[i];
+                    L.x += h;
+                    const double hmaxn = L.tout;  // tout - t with t = 0
+                    if (::fabs(hnew) > hmaxn) hnew = hmaxn;
+                    if (L.reject) hnew = smin(::fabs(hnew), ::fabs(h));
+                    L.reject = false;
+                    L.h = hnew;
+                    L.fresh = true;
+                } else {
+                    L.reject = true;
+                    L.last = false;
+                    L.h = hnew;
+                    if (L.n_accept >= 1) L.n_reject += 1;
+                }
+            }
+        }
+    }
+    // integrated count: one atomic per warp
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) integrated += __shfl_xor_sync(0xffffffffu, integrated, off);
+    if ((threadIdx.x & 31) == 0 && integrated) atomicAdd(&ctl->integrated, integrated);
+}
+
+}  // namespace wr
