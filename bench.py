@@ -1,0 +1,333 @@
+#!/usr/bin/env python3
+"""Benchmark: cells/s of the 64^3 gridwide-independent primordial-chemistry collapse.
+
+One *step* is one full collapse of the grid: 64^3 = 262,144 cells from the
+reference's initial condition through the 1,000-outer-step free-fall schedule with
+seeded perturbations (the reference's config ``--grid 64``), plain FP64 with the
+library's portable exp/log.  The metric is the reference's: cells / integration
+time (reproducer.cpp:8626-8651; published 15,055 cells/s on H200,
+docs/performance/optimization-results.md:51).
+
+  value   device time (CUDA events on the library's stream) of the run with the
+          state already in HBM; L2 is flushed (256 MiB write) before each timed step
+  e2e     the same through the public API with host buffers: create, H2D of the
+          216-byte records, run, D2H, destroy (wall clock)
+  roofline  the advance kernel, FP64-bound: algorithmic FP64 work (the reference's
+          source-level operation counts, weighted exp/log = 25, sqrt/cbrt = 20,
+          + - * / = 1, times the per-cell Jacobian and attempt counters) over its
+          event-timed duration, against this GPU's measured FP64 FMA rate
+  cpu_baseline  the CPU oracle with C-library math (bitwise the reference's CPU
+          arithmetic) on all host cores, on a 16^3 full collapse
+
+``--impl reference`` times the reference's CPU path (the same oracle) instead:
+each step is an 8^3 full collapse on all host cores.
+
+Multi-GPU: the path does not shard (every outer step needs the grid-wide minimum
+over all cells); N > 1 runs N independent replicas, one per GPU.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PUBLISHED_CELLS_PER_S = 15055.0  # H200, the benchmark spec
+F_JAC_EXTRA = 104   # burn_state_from_y before each Jacobian (eos_re sums), reproducer.cpp:7029-7038
+F_RHS_EXTRA = 104   # the same before each RHS
+F_LU = 2149         # lu_decomposition<15>: sum_{m=1..14} (1 div + m mul + 2 m^2), reproducer.cpp:96-151
+F_SOLVE = 435       # lu_solve<15>: 210 forward + 15 div + 210 backward, reproducer.cpp:154-181
+F_ATTEMPT = 541     # stage combinations 375, error norm 96, controller + E = -J + I/(h gamma) 70
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0, None
+    import torch
+    import torch.distributed as tdist
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    torch.cuda.set_device(local)
+    tdist.init_process_group("nccl")
+    return rank, ws, local, tdist
+
+
+def _barrier(tdist):
+    if tdist is not None:
+        import torch
+        torch.cuda.synchronize()
+        tdist.barrier()
+        torch.cuda.synchronize()
+
+
+def _max_over_ranks(tdist, value):
+    if tdist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_ops(cells):
+    """Weighted FP64 operations of the reference algorithm for the work the cells did."""
+    from warp_reactor_gb300.gen import build_network, ir_io
+    c = build_network.op_counts(ir_io.load())
+    f_j = c["source_jac_weighted"] + F_JAC_EXTRA
+    f_rhs = c["source_rhs_weighted"] + F_RHS_EXTRA
+    f_att = 3 * f_rhs + F_LU + 3 * F_SOLVE + F_ATTEMPT
+    st = cells["stats"]
+    nj = float(st["jacobian_calls"].sum())
+    na = float(st["internal_steps"].sum())
+    return nj * f_j + na * f_att, {"F_J": f_j, "F_RHS": f_rhs, "F_attempt": f_att, "jacobians": nj, "attempts": na}
+
+
+def cpu_baseline(grid, threads):
+    from oracle import oracle
+    o = oracle.load("libm")
+    cells = o.make_grid(grid)
+    t0 = time.perf_counter()
+    rc, cgs = o.run(cells, perturb=True, nthreads=threads)
+    dt = time.perf_counter() - t0
+    if rc != 1:
+        raise RuntimeError(f"CPU oracle failed with {rc}")
+    return len(cells) / dt, dt, cgs
+
+
+def run_reference(args, rank, ws, tdist):
+    if rank != 0:
+        return 0
+    from warp_reactor_gb300 import build
+    build.generate_network()
+    build.build_oracle()
+    threads = os.cpu_count() or 1
+    grid = args.ref_grid
+    for _ in range(args.warmup):
+        cpu_baseline(grid, threads)
+    times = []
+    n = grid ** 3
+    for _ in range(args.steps):
+        _, dt, cgs = cpu_baseline(grid, threads)
+        times.append(dt)
+    total = sum(times)
+    value = args.steps * n / total
+    line = {
+        "impl": "reference", "metric": "cells/s, 64^3 collapse", "value": value, "unit": "cells/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{grid}^3 gridwide-independent full collapse (sample of the 64^3 workload), "
+                               "reference CPU arithmetic", "grid": grid, "outer_steps": cgs,
+                   "parallelism": f"cpu{threads}"},
+        "cpu_baseline": {"value": value, "unit": "cells/s", "cores": threads, "kind": "port",
+                         "sample": f"{grid}^3 full collapse per step, C-library math (bitwise the reference CPU "
+                                   f"build), OpenMP over cells"},
+        "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args, rank, ws, local, tdist):
+    import warp_reactor_gb300 as wr
+    from warp_reactor_gb300 import build
+    build.build_all()
+    math_mode = wr.MATH_CUDA if args.math == "cuda" else wr.MATH_PORTABLE
+    grid = args.grid
+    cells0 = wr.make_grid(grid)
+    n = len(cells0)
+    ctx = wr.Context(n, local, math_mode)
+    ctx.set_profiling(True)
+    out = np.empty_like(cells0)
+
+    def one_step():
+        ctx.upload(cells0)
+        wr.lib().wr_diag_flush_l2(256)
+        rc, cgs = ctx.run(True)
+        if rc != wr.SUCCESS:
+            raise RuntimeError(f"run failed with {rc}: {wr.last_error()}")
+        return ctx.run_timing(), cgs
+
+    for _ in range(args.warmup):
+        one_step()
+    _barrier(tdist)
+    launches0 = wr.kernel_launch_count()
+    timings = []
+    with ClockSampler(local) as clocks:
+        t_wall = time.perf_counter()
+        for _ in range(args.steps):
+            t, cgs = one_step()
+            timings.append(t)
+        t_wall = time.perf_counter() - t_wall
+    launches = wr.kernel_launch_count() - launches0
+    _barrier(tdist)
+    run_s = sum(t.run_ms for t in timings) / 1e3
+    run_s = _max_over_ranks(tdist, run_s)
+    value = ws * args.steps * n / run_s
+    ctx.download(out)
+    adv_ms = sum(t.advance_ms for t in timings)
+    adv_launches = sum(t.advance_launches for t in timings)
+    ops, opinfo = algorithmic_ops(out)
+    peak = wr.fp64_peak()
+    achieved = ops * args.steps / (adv_ms / 1e3)
+
+    # e2e through the public API with host buffers (timed on the host)
+    e2e_cells = cells0.copy()
+    _barrier(tdist)
+    t0 = time.perf_counter()
+    rc, _ = wr.run_cells(e2e_cells, True, math_mode, local)
+    e2e_s = _max_over_ranks(tdist, time.perf_counter() - t0)
+    if rc != wr.SUCCESS:
+        raise RuntimeError(f"e2e run failed with {rc}")
+    ctx.close()
+    if rank != 0:
+        return 0
+    cpu = None
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, dt, _ = cpu_baseline(args.cpu_grid, threads)
+        cpu = {"value": v, "unit": "cells/s", "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_grid}^3 full collapse ({args.cpu_grid ** 3} cells, {dt:.1f} s), CPU oracle with "
+                         f"C-library math (bitwise the reference CPU build), OpenMP over cells"}
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "k_advance_grid64_traffic.txt")
+    if os.path.exists(tpath):
+        for ln in open(tpath):
+            if ln.startswith("bytes_per_launch:"):
+                traffic = float(ln.split(":", 1)[1])
+    line = {
+        "metric": "cells/s, 64^3 collapse", "value": value, "unit": "cells/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * run_s / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": value / ws / PUBLISHED_CELLS_PER_S if ws == 1 else None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{grid}^3 gridwide-independent collapse, 1000 outer steps, perturbations on, "
+                               f"plain FP64, {args.math} exp/log", "grid": grid, "cells": n, "outer_steps": cgs,
+                   "form": "plain-fp64 persistent lane-refill advance", "l2": "flushed (256 MiB write) before each step",
+                   "parallelism": f"replicas{ws}"},
+        "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12,
+                     "unit": "T FP64-op/s (weighted, FMA instruction = 1)", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": "measured live: wr_diag_fp64_peak (DFMA chains, all SMs)",
+                     "kernel": "k_advance", "launches": adv_launches,
+                     "ms_per_launch": adv_ms / max(adv_launches, 1), "algorithmic_ops_per_step": ops, **opinfo},
+        "cpu_baseline": cpu,
+        "e2e": {"value": ws * n / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": n * 216,
+                "d2h_bytes_per_step": n * 216},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+        "wall_s_timed": t_wall,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def profile_steps(args):
+    """A short, fixed run for ncu: ``--profile-steps S`` outer steps of the grid
+    through wr_prepare / wr_advance (the same kernels as wr_run)."""
+    import warp_reactor_gb300 as wr
+    from warp_reactor_gb300 import build
+    build.build_all()
+    cells = wr.make_grid(args.grid)
+    math_mode = wr.MATH_CUDA if args.math == "cuda" else wr.MATH_PORTABLE
+    with wr.Context(len(cells), 0, math_mode) as ctx:
+        ctx.upload(cells)
+        grid_time, done = 0.0, 0
+        for step in range(args.profile_steps):
+            rc, dt = ctx.prepare(done, grid_time, step, True)
+            if rc != wr.SUCCESS or dt == np.finfo(np.float64).max:
+                break
+            rc, cnt = ctx.advance(done, grid_time + dt, dt)
+            if rc != wr.SUCCESS or cnt == 0:
+                break
+            grid_time += dt
+            done += 1
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
+    ap.add_argument("--grid", type=int, default=64)
+    ap.add_argument("--math", choices=("portable", "cuda"), default="portable")
+    ap.add_argument("--cpu-grid", type=int, default=16)
+    ap.add_argument("--ref-grid", type=int, default=8)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="profiling driver: run this many outer steps host-stepped, print nothing, exit")
+    args = ap.parse_args()
+    if args.profile_steps > 0:
+        return profile_steps(args)
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+    rank, ws, local, tdist = _dist()
+    if args.impl == "reference":
+        return run_reference(args, rank, ws, tdist)
+    return run_gb300(args, rank, ws, local, tdist)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

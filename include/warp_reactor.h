@@ -124,6 +124,27 @@ int wr_advance(wr_ctx* ctx, int completed_global_steps, double next_grid_time,
  * as the starting count and receives the final count. */
 int wr_run(wr_ctx* ctx, int perturb, int* completed_global_steps);
 
+/* Copy the grid dt of each outer step of the last wr_run (the value the reference
+ * computes on the host at reproducer.cpp:7888-7893) into out[0..max_steps-1]. */
+int wr_dt_history(wr_ctx* ctx, double* out, int max_steps);
+
+/* Device-time breakdown of the last wr_run, measured with CUDA events on the
+ * context's stream (collected only after wr_set_profiling(ctx, 1)).  The
+ * reference times the whole run on the host (reproducer.cpp:8626-8651); these
+ * are the per-kernel figures behind that number. */
+typedef struct wr_run_timing {
+    double run_ms;        /* first launch to last launch of wr_run */
+    double prepare_ms;    /* sum over prepare launches */
+    double advance_ms;    /* sum over advance launches */
+    int32_t prepare_launches;
+    int32_t advance_launches;
+    int32_t outer_steps;  /* completed global steps of the run */
+    int32_t reserved_;
+} wr_run_timing;
+
+int wr_set_profiling(wr_ctx* ctx, int on);
+int wr_get_run_timing(wr_ctx* ctx, wr_run_timing* out);
+
 /* Drop-in for run_cells_cuda (reproducer.cpp:7791-7975): create, upload, run,
  * download, destroy, on the current CUDA device. */
 int wr_run_cells(wr_collapse_state* cells, int num_cells, int perturb,

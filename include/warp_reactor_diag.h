@@ -1,0 +1,55 @@
+/*
+ * warp_reactor_diag.h -- diagnostic entry points of the GB300 library.
+ *
+ * Each runs one piece of the device integrator on caller-supplied inputs so that
+ * tests can compare it with the CPU oracle and with the reference's own test
+ * fixtures.  Inputs and outputs are host arrays; the functions allocate and free
+ * their own device buffers and run on the current CUDA device.  Return values are
+ * IntegratorResult codes (WR_SUCCESS = 1).
+ */
+#ifndef WARP_REACTOR_DIAG_H
+#define WARP_REACTOR_DIAG_H
+
+#include "warp_reactor.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* The network at n burn states (X: n x 14 floored number densities, T: n
+ * temperatures): J (n x 225, row-major, the reference's jac(row+1, col+1)) and the
+ * fused RHS f_fused (n x 15) from one evaluation, and f_rhs (n x 15) from the
+ * RHS-only evaluation.  The reference computes these in actual_jac / actual_rhs
+ * (reproducer.cpp:6998-7011, 1515-1535).  math_mode is WR_MATH_PORTABLE or
+ * WR_MATH_CUDA. */
+int wr_diag_network(int n, const double* X, const double* T, int math_mode,
+                    double* J, double* f_fused, double* f_rhs);
+
+/* n independent 15x15 systems: LU factorisation with partial pivoting and the
+ * triangular solve, the device code of the advance kernel.  Replaces
+ * lu_decomposition<15> / lu_solve<15> (reproducer.cpp:96-181).  A and LU are
+ * n x 225 row-major, b and x are n x 15, ipvt and info are n x 15 and n.  The
+ * solve runs only where info == 0 (x = b otherwise). */
+int wr_diag_lu(int n, const double* A, const double* b, double* LU, int* ipvt, int* info, double* x);
+
+/* Elementwise exp (fn = 0), log (fn = 1) or cbrt (fn = 2) of n values on the
+ * device with the given math mode: the functions std::exp / std::log / std::cbrt
+ * of the reference's network and controller (reproducer.cpp:342-6994, 7309). */
+int wr_diag_math(int n, const double* x, int fn, int math_mode, double* out);
+
+/* Evict the GPU's L2 cache by writing `mib` MiB of device memory (a buffer kept
+ * for the life of the process), so a following timed run starts cold like the
+ * reference's first launch.  No reference counterpart (benchmark hygiene). */
+int wr_diag_flush_l2(int mib);
+
+/* Measured FP64 throughput of this GPU: independent FMA chains in every lane of a
+ * full grid, timed with CUDA events.  *dfma_per_s receives FP64 FMA instructions
+ * per second per GPU (one FMA = 2 FLOP).  No reference counterpart: the roofline
+ * denominator of the reference's FP64-bound path, measured on the same device. */
+int wr_diag_fp64_peak(double* dfma_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WARP_REACTOR_DIAG_H */

@@ -609,4 +609,29 @@ int wro_run(wr_collapse_state* cells, int n, int perturb, int* cgs, int max_step
     return result;
 }
 
+// Replays a subset of cells through a recorded grid-timestep history: cell_ids[i]
+// is the grid index of cells[i] (the perturbation seed), dt_hist[s] the grid dt of
+// outer step s.  Cells are independent given the grid dt, so a sample of a large
+// grid can be checked against the GPU run without integrating the whole grid.
+// Returns the first failure code; *cgs receives the number of steps replayed.
+int wro_replay(wr_collapse_state* cells, const int* cell_ids, int n, int perturb,
+               const double* dt_hist, int nsteps, int nthreads) {
+    std::atomic<int> failure{WR_SUCCESS};
+    double grid_time = 0.0;
+    for (int step = 0; step < nsteps; ++step) {
+        const double dt_grid = dt_hist[step];
+        const double next = grid_time + dt_grid;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads > 0 ? nthreads : 1)
+        for (int i = 0; i < n; ++i) {
+            double cand;
+            prepare_cell(cells[i], cell_ids[i], step, grid_time, step, perturb != 0, cand, failure);
+            if (cand != DBL_MAX && cand < dt_grid) record_failure(failure, WR_BAD_INPUTS);
+            advance_cell(cells[i], step, next, dt_grid, failure);
+        }
+        if (failure.load() != WR_SUCCESS) break;
+        grid_time = next;
+    }
+    return failure.load();
+}
+
 }  // extern "C"

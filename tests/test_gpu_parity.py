@@ -1,0 +1,189 @@
+"""GPU parity: the CUDA library through its C ABI against the CPU oracle.
+
+Integer/index results (steps, counters, pivots) must match exactly.  The library's
+default (portable) arithmetic is the oracle's, so floating-point results must match
+bit for bit too; the CUDA-libm mode is compared with the reference's own CUDA
+kernel outputs (fixtures from the reference run on GB300).
+"""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+pytestmark = pytest.mark.gpu
+
+
+def _diag_network(wr, X, T, math):
+    L = wr.lib()
+    L.wr_diag_network.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 2 + [ctypes.c_int] + [ctypes.c_void_p] * 3
+    n = len(T)
+    X = np.ascontiguousarray(X, np.float64)
+    T = np.ascontiguousarray(T, np.float64)
+    J = np.zeros((n, 15, 15))
+    f = np.zeros((n, 15))
+    g = np.zeros((n, 15))
+    assert L.wr_diag_network(n, X.ctypes.data, T.ctypes.data, math, J.ctypes.data, f.ctypes.data, g.ctypes.data) == 1
+    return J, f, g
+
+
+def _states(n, seed):
+    rng = np.random.default_rng(seed)
+    return 10.0 ** rng.uniform(-40, 18, size=(n, 14)), 10.0 ** rng.uniform(0.5, 5.0, size=n)
+
+
+def test_network_portable_bitwise(wr, gpu, oracle_port):
+    g = np.load(os.path.join(GOLDEN, "network_ref.npz"))
+    Xr, Tr = _states(2000, 99)
+    X = np.vstack([g["X"], Xr])
+    T = np.concatenate([g["T"], Tr])
+    J, f, f2 = _diag_network(wr, X, T, wr.MATH_PORTABLE)
+    assert f.tobytes() == f2.tobytes()  # the fused J+RHS evaluation gives the RHS-only values
+    for i in range(len(T)):
+        Jo, fo = oracle_port.net_jac(X[i], T[i])
+        assert J[i].tobytes() == Jo.tobytes(), i
+        assert f[i].tobytes() == fo.tobytes(), i
+
+
+def test_network_cuda_math_close_to_reference(wr, gpu):
+    """CUDA's exp/log are not the C library's: values agree to a few ulps."""
+    g = np.load(os.path.join(GOLDEN, "network_ref.npz"))
+    J, f, _ = _diag_network(wr, g["X"], g["T"], wr.MATH_CUDA)
+    for ours, ref in ((J.reshape(len(J), -1), g["J"].reshape(len(J), -1)), (f, g["f"])):
+        big = np.abs(ref) > 1e-280
+        rel = np.abs(ours[big] - ref[big]) / np.abs(ref[big])
+        assert np.median(rel) < 1e-15 and rel.max() < 1e-9
+
+
+def test_lu_fixtures_bitwise(wr, gpu):
+    g = np.load(os.path.join(GOLDEN, "lu_ref.npz"))
+    rng = np.random.default_rng(7)
+    extra = rng.normal(size=(61, 15, 15)) + 3 * np.eye(15)
+    A = np.ascontiguousarray(np.concatenate([g["A"], extra]))
+    b = np.ascontiguousarray(np.concatenate([g["b"], rng.normal(size=(61, 15))]))
+    n = len(A)
+    LU = np.zeros_like(A)
+    ip = np.zeros((n, 15), np.int32)
+    info = np.zeros(n, np.int32)
+    x = np.zeros_like(b)
+    L = wr.lib()
+    L.wr_diag_lu.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 6
+    assert L.wr_diag_lu(n, A.ctypes.data, b.ctypes.data, LU.ctypes.data, ip.ctypes.data, info.ctypes.data,
+                        x.ctypes.data) == 1
+    assert (info[:8] == g["info"]).all()
+    assert LU[:8].tobytes() == g["LU"].tobytes()
+    assert (ip[:8] == g["ipvt"]).all()
+    ok = g["info"] == 0
+    assert x[:8][ok].tobytes() == g["x"][ok].tobytes()
+    from oracle import oracle
+    o = oracle.load("port")
+    for i in range(8, n):
+        inf, LUo, ipo = o.lu(A[i])
+        assert inf == info[i] and LUo.tobytes() == LU[i].tobytes() and (ipo == ip[i]).all()
+        assert o.lu_solve(LUo, ipo, b[i]).tobytes() == x[i].tobytes()
+
+
+@pytest.mark.parametrize("grid,perturb", [(1, True), (2, True), (3, True), (4, True), (5, True), (2, False),
+                                          (8, True)])
+def test_grid_runs_bitwise(wr, gpu, oracle_port, grid, perturb):
+    cells = wr.make_grid(grid)
+    rc, cgs = wr.run_cells(cells, perturb)
+    ref = oracle_port.make_grid(grid)
+    rc_o, cgs_o = oracle_port.run(ref, perturb=perturb)
+    assert rc == rc_o == wr.SUCCESS
+    assert cgs == cgs_o
+    assert (cells["completed_steps"] == ref["completed_steps"]).all()
+    assert (cells["stats"] == ref["stats"]).all()  # substep counts
+    assert cells.tobytes() == ref.tobytes()
+
+
+def test_host_stepped_api_equals_device_loop(wr, gpu):
+    """wr_prepare / wr_advance driven from the host like run_cells_cuda's loop
+    (reproducer.cpp:7859-7959) gives the same states as the device-driven wr_run."""
+    grid = 3
+    a = wr.make_grid(grid)
+    rc, cgs = wr.run_cells(a, True)
+    b = wr.make_grid(grid)
+    with wr.Context(len(b)) as ctx:
+        ctx.upload(b)
+        grid_time, done = 0.0, 0
+        for step in range(wr.MAX_COLLAPSE_STEPS):
+            r, dt = ctx.prepare(done, grid_time, step, True)
+            assert r == wr.SUCCESS
+            if dt == np.finfo(np.float64).max:
+                break
+            r, n = ctx.advance(done, grid_time + dt, dt)
+            assert r == wr.SUCCESS
+            if n == 0:
+                break
+            grid_time += dt
+            done += 1
+        ctx.download(b)
+    assert done == cgs
+    assert a.tobytes() == b.tobytes()
+
+
+@pytest.mark.parametrize("grid", [4, 8])
+def test_cuda_math_equals_reference_cuda_kernel(wr, gpu, grid):
+    """WR_MATH_CUDA reproduces the reference's own CUDA kernels (reproducer.cpp
+    compiled with nvcc --fmad=false for sm_103a and run on GB300) bit for bit."""
+    path = os.path.join(GOLDEN, f"refcuda_grid{grid}.bin")
+    ref = np.fromfile(path, wr.PACKED_FINAL_STATE)
+    cells = wr.make_grid(grid)
+    rc, cgs = wr.run_cells(cells, True, math=wr.MATH_CUDA)
+    assert rc == wr.SUCCESS
+    assert wr.pack_final_states(cells, grid).tobytes() == ref.tobytes()
+
+
+def test_failure_bad_inputs_is_reported(wr, gpu):
+    """A host-made invalid cell (zero density, reproducer.cpp:7721-7725) ends the
+    run with BAD_INPUTS, like the reference; the context stays usable."""
+    cells = wr.make_grid(2)
+    cells["xn"][5] = 0.0
+    with wr.Context(len(cells)) as ctx:
+        ctx.upload(cells)
+        rc, cgs = ctx.run(True)
+        assert rc == wr.BAD_INPUTS and cgs == 0
+        good = wr.make_grid(2)
+        ctx.upload(good)
+        rc, cgs = ctx.run(True)
+        assert rc == wr.SUCCESS and cgs == 1000
+
+
+def test_failure_time_mismatch(wr, gpu):
+    cells = wr.make_grid(2)
+    cells["time"][3] = 1.0  # a participating cell out of step with the grid clock
+    rc, cgs = wr.run_cells(cells, True)
+    assert rc == wr.BAD_INPUTS and cgs == 0
+
+
+def test_full_grid_64_replay_sample(wr, gpu, oracle_port):
+    """64^3 (the benchmark size): the oracle replays a sample of cells through the
+    GPU's grid-dt history and must reproduce them bit for bit; the sample includes
+    the cells that set the grid dt."""
+    grid = 64
+    cells = wr.make_grid(grid)
+    with wr.Context(len(cells)) as ctx:
+        ctx.upload(cells)
+        rc, cgs = ctx.run(True)
+        hist = np.zeros(wr.MAX_COLLAPSE_STEPS)
+        L = wr.lib()
+        L.wr_dt_history.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        assert L.wr_dt_history(ctx.handle, hist.ctypes.data, len(hist)) == 1
+        ctx.download(cells)
+    assert rc == wr.SUCCESS and cgs == 1000
+    rng = np.random.default_rng(64)
+    ids = np.unique(np.concatenate([[0, len(cells) - 1], rng.choice(len(cells), 48, replace=False)]))
+    sample = np.repeat(oracle_port.make_grid(1), len(ids))
+    lib = oracle_port.lib
+    lib.wro_replay.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                               ctypes.c_int, ctypes.c_int]
+    ids32 = np.ascontiguousarray(ids, np.int32)
+    r = lib.wro_replay(sample.ctypes.data, ids32.ctypes.data, len(ids), 1, hist.ctypes.data, cgs, os.cpu_count())
+    assert r == 1
+    assert sample.tobytes() == cells[ids].tobytes()
+    # grid-wide invariants
+    assert np.isfinite(cells["T"]).all() and (cells["xn"] > 0).all()
+    live = cells["completed_steps"] == cgs
+    assert (cells["time"][live] == cells["time"][live][0]).all()

@@ -55,6 +55,13 @@ PACKED_FINAL_STATE = np.dtype([
 assert PACKED_FINAL_STATE.itemsize == 172
 
 
+class RunTiming(ctypes.Structure):
+    """wr_run_timing: device-time breakdown of the last wr_run."""
+    _fields_ = [("run_ms", ctypes.c_double), ("prepare_ms", ctypes.c_double), ("advance_ms", ctypes.c_double),
+                ("prepare_launches", ctypes.c_int32), ("advance_launches", ctypes.c_int32),
+                ("outer_steps", ctypes.c_int32), ("reserved_", ctypes.c_int32)]
+
+
 class WarpReactorError(RuntimeError):
     def __init__(self, code: int, what: str):
         super().__init__(f"{what} failed with IntegratorResult {code}")
@@ -84,6 +91,10 @@ def lib() -> ctypes.CDLL:
         L.wr_run_cells.argtypes = [vp, ctypes.c_int, ctypes.c_int, ip]
         L.wr_make_collapse_state.argtypes = [vp]
         L.wr_make_collapse_state.restype = None
+        L.wr_set_profiling.argtypes = [vp, ctypes.c_int]
+        L.wr_get_run_timing.argtypes = [vp, ctypes.POINTER(RunTiming)]
+        L.wr_dt_history.argtypes = [vp, vp, ctypes.c_int]
+        L.wr_diag_fp64_peak.argtypes = [dp]
         L.wr_last_error.restype = ctypes.c_char_p
         L.wr_kernel_launch_count.restype = ctypes.c_uint64
         _lib = L
@@ -169,6 +180,23 @@ class Context:
         rc = lib().wr_advance(self.handle, completed_global_steps, next_grid_time, dt_grid, ctypes.byref(cnt))
         return rc, cnt.value
 
+    def set_profiling(self, on: bool = True) -> None:
+        rc = lib().wr_set_profiling(self.handle, int(bool(on)))
+        if rc != SUCCESS:
+            raise WarpReactorError(rc, f"wr_set_profiling ({last_error()})")
+
+    def run_timing(self) -> RunTiming:
+        t = RunTiming()
+        lib().wr_get_run_timing(self.handle, ctypes.byref(t))
+        return t
+
+    def dt_history(self) -> np.ndarray:
+        out = np.zeros(MAX_COLLAPSE_STEPS)
+        rc = lib().wr_dt_history(self.handle, out.ctypes.data, MAX_COLLAPSE_STEPS)
+        if rc != SUCCESS:
+            raise WarpReactorError(rc, f"wr_dt_history ({last_error()})")
+        return out
+
     def run(self, perturb: bool = True, completed_global_steps: int = 0):
         """The whole outer loop on the device -> (result, completed_global_steps)."""
         cgs = ctypes.c_int(completed_global_steps)
@@ -184,6 +212,15 @@ def run_cells(cells: np.ndarray, perturb: bool = True, math: int = MATH_PORTABLE
         rc, cgs = ctx.run(perturb)
         ctx.download(cells)
     return rc, cgs
+
+
+def fp64_peak() -> float:
+    """Measured FP64 FMA instructions per second of the current GPU."""
+    v = ctypes.c_double()
+    rc = lib().wr_diag_fp64_peak(ctypes.byref(v))
+    if rc != SUCCESS:
+        raise WarpReactorError(rc, "wr_diag_fp64_peak")
+    return v.value
 
 
 def pack_final_states(cells: np.ndarray, grid_dim: int) -> np.ndarray:

@@ -34,7 +34,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompil
                      "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE, "-I", CSRC]
 CXX_FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fPIC"]
 
-CUDA_UNITS = ["wr_capi.cu", "wr_adv_portable.cu", "wr_adv_cuda.cu"]
+CUDA_UNITS = ["wr_capi.cu", "wr_adv_portable.cu", "wr_adv_cuda.cu", "wr_diag.cu"]
 
 
 def _nvcc() -> str:
@@ -71,7 +71,7 @@ def generate_network() -> str:
 
 def _headers():
     return (glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) +
-            glob.glob(os.path.join(CSRC, "generated", "*.h")) + [os.path.join(INCLUDE, "warp_reactor.h")])
+            glob.glob(os.path.join(CSRC, "generated", "*.h")) + glob.glob(os.path.join(INCLUDE, "*.h")))
 
 
 def build_library(verbose=False, jobs=None) -> str:
@@ -128,7 +128,11 @@ def build_reference_oracle(verbose=False) -> None:
     """Compile the reference itself into oracle/_ref (only where its tree exists)."""
     script = os.path.join(ORACLE, "build_ref.sh")
     ref_dir = os.environ.get("REF_DIR", "/root/reference")
-    if os.path.exists(os.path.join(ref_dir, "reproducer.cpp")) and os.path.exists(script):
+    ref_src = os.path.join(ref_dir, "reproducer.cpp")
+    if not (os.path.exists(ref_src) and os.path.exists(script)):
+        return
+    deps = [ref_src, script, os.path.join(ORACLE, "ref_shim.cpp"), os.path.join(INCLUDE, "warp_reactor.h")]
+    if _stale(os.path.join(ORACLE, "_ref", "libwr_ref.so"), deps):
         _run(["sh", script], verbose)
 
 

@@ -50,7 +50,13 @@ struct wr_ctx {
     StepCtl* ctl = nullptr;
     StepCtl* host_ctl = nullptr;  // pinned mirror
     double* jbackup = nullptr;
+    double* dt_hist = nullptr;  // grid dt of every outer step of the last wr_run
     wr_collapse_state* staging = nullptr;  // device AoS records for upload/download
+    // optional per-kernel timing of wr_run (CUDA events on the context stream)
+    bool profiling = false;
+    cudaEvent_t ev[4 * WR_MAX_COLLAPSE_STEPS + 2] = {};
+    int ev_used = 0;
+    wr_run_timing timing{};
 };
 
 namespace wr {
@@ -120,7 +126,7 @@ __global__ void k_begin_advance(StepCtl* ctl, int cgs, double next_grid_time, do
 }
 
 // host checks between prepare and advance, reproducer.cpp:7880-7909
-__global__ void k_decide(StepCtl* ctl) {
+__global__ void k_decide(StepCtl* ctl, double* dt_hist) {
     if (ctl->stop) return;
     if (ctl->failure != WR_SUCCESS) {
         ctl->stop = 1;
@@ -141,6 +147,7 @@ __global__ void k_decide(StepCtl* ctl) {
     ctl->next_grid_time = next;
     ctl->integrated = 0;
     ctl->queue = 0;
+    if (ctl->step >= 0 && ctl->step < WR_MAX_COLLAPSE_STEPS) dt_hist[ctl->step] = dt;
 }
 
 // host bookkeeping after the advance, reproducer.cpp:7930-7958
@@ -164,6 +171,10 @@ namespace {
 int set_device(wr_ctx* ctx) {
     const cudaError_t e = cudaSetDevice(ctx->device);
     return e == cudaSuccess ? WR_SUCCESS : fail("cudaSetDevice", e);
+}
+
+void record(wr_ctx* ctx, int idx) {
+    if (ctx->profiling) cudaEventRecord(ctx->ev[idx], ctx->stream);
 }
 
 cudaError_t launch_advance(wr_ctx* ctx) {
@@ -225,6 +236,7 @@ int wr_create(int num_cells, int device, int math_mode, wr_ctx** out) {
     e = cudaMalloc(&ctx->state_buf, bytes);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->ctl, sizeof(StepCtl));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->jbackup, nslots * NEQ * NEQ * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->dt_hist, WR_MAX_COLLAPSE_STEPS * sizeof(double));
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->host_ctl, sizeof(StepCtl));
     if (e == cudaSuccess) e = ctx->math == WR_MATH_CUDA ? configure_advance_cuda() : configure_advance_portable();
     if (e != cudaSuccess) {
@@ -263,9 +275,11 @@ void wr_destroy(wr_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->profiling) wr_set_profiling(ctx, 0);
     cudaFree(ctx->state_buf);
     cudaFree(ctx->ctl);
     cudaFree(ctx->jbackup);
+    cudaFree(ctx->dt_hist);
     cudaFree(ctx->staging);
     cudaFreeHost(ctx->host_ctl);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -346,14 +360,23 @@ int wr_run(wr_ctx* ctx, int perturb, int* completed_global_steps) {
     int rc = set_device(ctx);
     if (rc != WR_SUCCESS) return rc;
     g_launches.fetch_add(1, std::memory_order_relaxed);
+    const int nev = 4 * WR_MAX_COLLAPSE_STEPS + 2;
+    ctx->ev_used = 0;
+    record(ctx, nev - 2);
     k_begin_step<<<1, 1, 0, ctx->stream>>>(ctx->ctl, *completed_global_steps, 0.0, 0, perturb ? 1 : 0);
+    int steps_launched = 0;
     for (int step = 0; step < WR_MAX_COLLAPSE_STEPS; ++step) {
+        record(ctx, 4 * step + 0);
         cudaError_t e = launch_prepare(ctx);
+        record(ctx, 4 * step + 1);
         if (e == cudaSuccess) {
             g_launches.fetch_add(1, std::memory_order_relaxed);
-            k_decide<<<1, 1, 0, ctx->stream>>>(ctx->ctl);
+            k_decide<<<1, 1, 0, ctx->stream>>>(ctx->ctl, ctx->dt_hist);
+            record(ctx, 4 * step + 2);
             e = launch_advance(ctx);
+            record(ctx, 4 * step + 3);
         }
+        steps_launched = step + 1;
         if (e == cudaSuccess) {
             g_launches.fetch_add(1, std::memory_order_relaxed);
             k_finalize<<<1, 1, 0, ctx->stream>>>(ctx->ctl, WR_MAX_COLLAPSE_STEPS);
@@ -366,10 +389,63 @@ int wr_run(wr_ctx* ctx, int perturb, int* completed_global_steps) {
             if (ctx->host_ctl->stop) break;
         }
     }
+    record(ctx, nev - 1);
     rc = read_ctl(ctx);
     if (rc != WR_SUCCESS) return rc;
+    if (ctx->profiling) {
+        wr_run_timing t{};
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, ctx->ev[nev - 2], ctx->ev[nev - 1]);
+        t.run_ms = ms;
+        for (int s = 0; s < steps_launched; ++s) {
+            cudaEventElapsedTime(&ms, ctx->ev[4 * s + 0], ctx->ev[4 * s + 1]);
+            t.prepare_ms += ms;
+            cudaEventElapsedTime(&ms, ctx->ev[4 * s + 2], ctx->ev[4 * s + 3]);
+            t.advance_ms += ms;
+        }
+        t.advance_launches = steps_launched;
+        t.prepare_launches = steps_launched;
+        t.outer_steps = ctx->host_ctl->cgs;
+        ctx->timing = t;
+    }
     *completed_global_steps = ctx->host_ctl->cgs;
     return ctx->host_ctl->failure;
+}
+
+int wr_set_profiling(wr_ctx* ctx, int on) {
+    if (!ctx) return fail_msg("wr_set_profiling: null context");
+    int rc = set_device(ctx);
+    if (rc != WR_SUCCESS) return rc;
+    if (on && !ctx->profiling) {
+        for (auto& ev : ctx->ev) {
+            const cudaError_t e = cudaEventCreate(&ev);
+            if (e != cudaSuccess) return fail("cudaEventCreate", e);
+        }
+    }
+    if (!on && ctx->profiling) {
+        for (auto& ev : ctx->ev) {
+            cudaEventDestroy(ev);
+            ev = nullptr;
+        }
+    }
+    ctx->profiling = on != 0;
+    return WR_SUCCESS;
+}
+
+int wr_get_run_timing(wr_ctx* ctx, wr_run_timing* out) {
+    if (!ctx || !out) return fail_msg("wr_get_run_timing: null argument");
+    *out = ctx->timing;
+    return WR_SUCCESS;
+}
+
+int wr_dt_history(wr_ctx* ctx, double* out, int max_steps) {
+    if (!ctx || !out || max_steps < 0) return fail_msg("wr_dt_history: bad argument");
+    int rc = set_device(ctx);
+    if (rc != WR_SUCCESS) return rc;
+    const int n = max_steps < WR_MAX_COLLAPSE_STEPS ? max_steps : WR_MAX_COLLAPSE_STEPS;
+    cudaError_t e = cudaMemcpyAsync(out, ctx->dt_hist, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    return e == cudaSuccess ? WR_SUCCESS : fail("wr_dt_history", e);
 }
 
 int wr_run_cells(wr_collapse_state* cells, int num_cells, int perturb, int* completed_global_steps) {
