@@ -37,6 +37,12 @@ int wr_diag_lu(int n, const double* A, const double* b, double* LU, int* ipvt, i
  * of the reference's network and controller (reproducer.cpp:342-6994, 7309). */
 int wr_diag_math(int n, const double* x, int fn, int math_mode, double* out);
 
+/* Elementwise a[i] / b[i] with the device's integer-pipe division (the kernels'
+ * division everywhere in the integrator): must equal IEEE binary64 division bit
+ * for bit.  The reference divides with the hardware operator throughout
+ * (reproducer.cpp:96-181, 284-339, 7205-7347). */
+int wr_diag_div(int n, const double* a, const double* b, double* out);
+
 /* Evict the GPU's L2 cache by writing `mib` MiB of device memory (a buffer kept
  * for the life of the process), so a following timed run starts cold like the
  * reference's first launch.  No reference counterpart (benchmark hygiene). */

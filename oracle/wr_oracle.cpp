@@ -551,6 +551,9 @@ void wro_lu_solve(const double* LU, const int* ipvt, double* x) {
 double wro_exp(double x) { return OracleMath::exp(x); }
 double wro_log(double x) { return OracleMath::log(x); }
 double wro_cbrt(double x) { return OracleMath::cbrt(x); }
+#ifndef WR_ORACLE_LIBM
+double wro_div_int(double a, double b) { return wr_div_int(a, b); }
+#endif
 
 // burn_ros2s on one cell's burn state, stats accumulated into cell->stats
 int wro_burn(wr_collapse_state* cell, double dt) {

@@ -39,11 +39,21 @@ def test_network_portable_bitwise(wr, gpu, oracle_port):
     X = np.vstack([g["X"], Xr])
     T = np.concatenate([g["T"], Tr])
     J, f, f2 = _diag_network(wr, X, T, wr.MATH_PORTABLE)
-    assert f.tobytes() == f2.tobytes()  # the fused J+RHS evaluation gives the RHS-only values
+
+    def same(a, b):
+        # bit-identical, except that a NaN matches any NaN: x86 and the GPU write
+        # different default-NaN bit patterns for invalid operations (adversarial
+        # random states reach inf - inf; integration states never do)
+        a, b = np.asarray(a).ravel(), np.asarray(b).ravel()
+        return bool(((a.view(np.uint64) == b.view(np.uint64)) | (np.isnan(a) & np.isnan(b))).all())
+
+    assert same(f, f2)  # the fused J+RHS evaluation gives the RHS-only values
     for i in range(len(T)):
         Jo, fo = oracle_port.net_jac(X[i], T[i])
-        assert J[i].tobytes() == Jo.tobytes(), i
-        assert f[i].tobytes() == fo.tobytes(), i
+        assert same(J[i], Jo), i
+        assert same(f[i], fo), i
+    g_ok = np.isfinite(J[: len(g["T"])]).all()
+    assert g_ok  # the reference's own fixture states are all finite
 
 
 def test_network_cuda_math_close_to_reference(wr, gpu):

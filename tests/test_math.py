@@ -82,3 +82,43 @@ def test_device_equals_host_bitwise(wr, gpu, oracle_port, fn):
     f = (oracle_port.exp, oracle_port.log, oracle_port.cbrt)[fn]
     host = np.array([f(float(v)) for v in x])
     assert out.view(np.uint64).tolist() == host.view(np.uint64).tolist()
+
+
+def _div_cases(rng, n):
+    a = 10 ** rng.uniform(-300, 300, n) * rng.choice([-1.0, 1.0], n)
+    b = 10 ** rng.uniform(-300, 300, n) * rng.choice([-1.0, 1.0], n)
+    ma = rng.integers(2**52, 2**53, n).astype(np.float64) * 2.0**-52
+    mb = rng.integers(2**52, 2**53, n).astype(np.float64) * 2.0**-52
+    special = np.array([0.0, -0.0, 1.0, np.inf, -np.inf, np.nan, 5e-324, 2.2250738585072014e-308,
+                        1.7976931348623157e308, 3.0, 0.1])
+    sa, sb = np.meshgrid(special, special)
+    return (np.concatenate([a, ma, mb, np.nextafter(ma, 3.0), sa.ravel()]),
+            np.concatenate([b, mb, ma, mb, sb.ravel()]))
+
+
+def test_integer_division_is_ieee_on_host(oracle_port):
+    """wr_div_int (the device division) computed on the host equals a / b."""
+    import ctypes
+    f = oracle_port.lib.wro_div_int
+    f.restype, f.argtypes = ctypes.c_double, [ctypes.c_double, ctypes.c_double]
+    a, b = _div_cases(np.random.default_rng(23), 20000)
+    with np.errstate(all="ignore"):
+        want = a / b
+    got = np.array([f(float(x), float(y)) for x, y in zip(a, b)])
+    same = (got.view(np.uint64) == want.view(np.uint64)) | (np.isnan(got) & np.isnan(want))
+    assert same.all(), (a[~same][:3], b[~same][:3])
+
+
+@pytest.mark.gpu
+def test_integer_division_is_ieee_on_device(wr, gpu):
+    import ctypes
+    a, b = _div_cases(np.random.default_rng(29), 400000)
+    a, b = np.ascontiguousarray(a), np.ascontiguousarray(b)
+    out = np.zeros_like(a)
+    L = wr.lib()
+    L.wr_diag_div.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    assert L.wr_diag_div(len(a), a.ctypes.data, b.ctypes.data, out.ctypes.data) == 1
+    with np.errstate(all="ignore"):
+        want = a / b
+    same = (out.view(np.uint64) == want.view(np.uint64)) | (np.isnan(out) & np.isnan(want))
+    assert same.all(), (a[~same][:3], b[~same][:3])

@@ -87,6 +87,11 @@ __global__ void k_fp64_peak(double* out, double a, double b) {
     out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 
+__global__ void k_diag_div(int n, const double* __restrict__ a, const double* __restrict__ b, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = ddiv(a[i], b[i]);
+}
+
 thread_local std::string g_diag_error;
 
 struct DevBuf {
@@ -171,6 +176,22 @@ int wr_diag_math(int n, const double* x, int fn, int math_mode, double* out) {
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpy(out, dout.p, nn * 8, cudaMemcpyDeviceToHost);
     return e == cudaSuccess ? WR_SUCCESS : diag_fail("wr_diag_math", e);
+}
+
+int wr_diag_div(int n, const double* a, const double* b, double* out) {
+    if (n <= 0 || !a || !b || !out) return WR_BAD_INPUTS;
+    const size_t nn = static_cast<size_t>(n);
+    DevBuf da, db, dout;
+    cudaError_t e = cudaMalloc(&da.p, nn * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&db.p, nn * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&dout.p, nn * 8);
+    if (e == cudaSuccess) e = cudaMemcpy(da.p, a, nn * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(db.p, b, nn * 8, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return diag_fail("wr_diag_div setup", e);
+    k_diag_div<<<(n + 255) / 256, 256>>>(n, (double*)da.p, (double*)db.p, (double*)dout.p);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(out, dout.p, nn * 8, cudaMemcpyDeviceToHost);
+    return e == cudaSuccess ? WR_SUCCESS : diag_fail("wr_diag_div", e);
 }
 
 int wr_diag_flush_l2(int mib) {

@@ -96,7 +96,7 @@ struct PortableMathCall {
     static __device__ __forceinline__ double cbrt(double x) { return wr_cbrt(x); }
     static __device__ __forceinline__ double sqrt(double x) { return ::sqrt(x); }
     static __device__ __forceinline__ double fabs(double x) { return ::fabs(x); }
-    static __device__ __forceinline__ double div(double a, double b) { return a / b; }
+    static __device__ __forceinline__ double div(double a, double b) { return wr_div_call(a, b); }
 };
 
 
@@ -145,8 +145,8 @@ __global__ void __launch_bounds__(B) k_prepare(DevState s, StepCtl* ctl) {
                 if (!valid_positive(dt) || !valid_positive(driver)) {
                     record_failure(ctl, WR_BAD_INPUTS);
                 } else if (dt < 10.0) {
-                    const double tff = dt / kTffReduc;
-                    driver += dt * (driver / tff);
+                    const double tff = ddiv(dt, kTffReduc);
+                    driver += dt * ddiv(driver, tff);
                 } else {
                     cand = static_cast<unsigned long long>(__double_as_longlong(dt));
                 }
@@ -230,7 +230,7 @@ __device__ __forceinline__ int lu_decompose(Mat<B> A, int* ip) {
                     A(k, j) = tr;
                 }
             }
-            const double mult = -1.0 / A(k, k);
+            const double mult = ddiv(-1.0, A(k, k));
             double l[NEQ];
 #pragma unroll
             for (int i = k + 1; i < NEQ; ++i) {
@@ -273,7 +273,7 @@ __device__ __forceinline__ void lu_solve(Mat<B> LU, const int* ip, double* x) {
 #pragma unroll
     for (int kb = 0; kb < NEQ; ++kb) {
         const int k = NEQ - 1 - kb;
-        x[k] = x[k] / LU(k, k);
+        x[k] = ddiv(x[k], LU(k, k));
         const double t = -x[k];
 #pragma unroll
         for (int j = 0; j < k; ++j) x[j] = x[j] + t * LU(j, k);
@@ -323,11 +323,11 @@ __global__ void __launch_bounds__(B, 1) k_advance(DevState s, StepCtl* ctl, doub
                 const double local_dt = collapse_timestep(xn);
                 if (local_dt < 10.0) continue;
                 const double old_density = s.driver[cell];
-                const double tff = local_dt / kTffReduc;
-                const double driver = old_density + dt_grid * (old_density / tff);
+                const double tff = ddiv(local_dt, kTffReduc);
+                const double driver = old_density + dt_grid * ddiv(old_density, tff);
                 s.driver[cell] = driver;
                 if (!valid_positive(driver) || driver > kDriverLimit) continue;
-                const double ratio = driver / old_density;
+                const double ratio = ddiv(driver, old_density);
 #pragma unroll
                 for (int k = 0; k < NS; ++k) xn[k] *= ratio;
                 const double rho = s.rho[cell] * ratio;
@@ -421,7 +421,7 @@ __global__ void __launch_bounds__(B, 1) k_advance(DevState s, StepCtl* ctl, doub
         // ---- one attempt of the inner loop, reproducer.cpp:7259-7345
         if (alive && have) {
             const double h = L.h;
-            const double fac = 1.0 / (h * kGamma);
+            const double fac = ddiv(1.0, h * kGamma);
 #pragma unroll
             for (int i = 0; i < NEQ; ++i) E(i, i) = E(i, i) + fac;
             const int info = lu_decompose<B>(E, ip);
@@ -457,13 +457,13 @@ __global__ void __launch_bounds__(B, 1) k_advance(DevState s, StepCtl* ctl, doub
 #pragma unroll
                         for (int i = 0; i < NEQ; ++i) {
                             yn[i] = y[i] + kA21 * ak1[i];
-                            w[i] = (kC21 / h) * ak1[i];
+                            w[i] = ddiv(kC21, h) * ak1[i];
                         }
                     } else {
 #pragma unroll
                         for (int i = 0; i < NEQ; ++i) {
                             yn[i] = y[i] + kA31 * ak1[i] + kA32 * ak2[i];
-                            w[i] = (kC31 * ak1[i] + kC32 * ak2[i]) / h;
+                            w[i] = ddiv(kC31 * ak1[i] + kC32 * ak2[i], h);
                         }
                     }
                     double X[NS], T, dy[NEQ];
@@ -488,21 +488,21 @@ __global__ void __launch_bounds__(B, 1) k_advance(DevState s, StepCtl* ctl, doub
                     const double rtol = i < NS ? kRtolSpec : kRtolEnergy;
                     const double atol = i < NS ? kAtolSpec : kAtolEnergy;
                     const double sk = atol + rtol * smax(::fabs(y[i]), ::fabs(ynew[i]));
-                    const double term = wi / sk;
+                    const double term = ddiv(wi, sk);
                     err += term * term;
                 }
-                err = ::sqrt(err / 15.0);
+                err = ::sqrt(ddiv(err, 15.0));
                 L.n_step += 1;
                 // step-size controller, reproducer.cpp:7308-7344
-                const double raw_fac = M::cbrt(err) / kSafe;
+                const double raw_fac = ddiv(M::cbrt(err), kSafe);
                 const double fac_step = smax(1.0 / kFacMax, smin(1.0 / kFacMin, raw_fac));
-                double hnew = h / fac_step;
+                double hnew = ddiv(h, fac_step);
                 if (err <= 1.0) {
                     L.n_accept += 1;
                     if (L.n_accept > 1) {
                         const double facgus = smax(1.0 / kFacMax,
-                            smin(1.0 / kFacMin, (L.hacc / h) * M::cbrt((err * err) / L.erracc) / kSafe));
-                        hnew = h / smax(fac_step, facgus);
+                            smin(1.0 / kFacMin, ddiv(ddiv(L.hacc, h) * M::cbrt(ddiv(err * err, L.erracc)), kSafe)));
+                        hnew = ddiv(h, smax(fac_step, facgus));
                     }
                     L.hacc = h;
                     L.erracc = smax(1.e-2, err);

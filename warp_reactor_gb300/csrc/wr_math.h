@@ -135,6 +135,60 @@ WR_MHD double wr_fixed_to_double(int64_t hi, uint64_t lo, int q) {
     return wr_from_bits(sign | (static_cast<uint64_t>(e2 + 1023) << 52) | (mant & 0x000fffffffffffffULL));
 }
 
+// Correctly rounded binary64 quotient a/b from integer arithmetic: the result is
+// the IEEE quotient (which is unique), so it can replace a/b anywhere without
+// changing a bit.  Normal operands with a normal quotient take the integer path:
+// a float reciprocal of the divisor's top 24 bits, two fixed-point Newton steps
+// (Q63), a 54-bit quotient, an exact remainder check and round-to-nearest-even.
+// Everything else (zeros, subnormals, inf/NaN, overflow/underflow) uses a / b.
+// On GB300 this keeps divisions off the FP64 pipe (a native double division
+// issues about eight FP64 instructions).
+WR_MHD double wr_div_int(double a, double b) {
+    const uint64_t ua = wr_bits(a), ub = wr_bits(b);
+    const uint32_t ea = static_cast<uint32_t>(ua >> 52) & 0x7ff;
+    const uint32_t eb = static_cast<uint32_t>(ub >> 52) & 0x7ff;
+    if (ea - 1u >= 2046u || eb - 1u >= 2046u) return a / b;
+    const uint64_t ma = (ua & 0x000fffffffffffffULL) | 0x0010000000000000ULL;
+    const uint64_t mb = (ub & 0x000fffffffffffffULL) | 0x0010000000000000ULL;
+    const int adj = ma < mb ? 1 : 0;
+    const int be = static_cast<int>(ea) - static_cast<int>(eb) - adj + 1023;
+    if (be < 1 || be > 2046) return a / b;
+    // y ~ 1/b_m in Q63, b_m = mb * 2^-52 in [1, 2)
+    const float bf = static_cast<float>(static_cast<uint32_t>(mb >> 29));  // exact, 24 bits
+#if defined(__CUDA_ARCH__)
+    const float rf = __frcp_rn(bf);
+#else
+    const float rf = 1.0f / bf;
+#endif
+    uint64_t Y = static_cast<uint64_t>(static_cast<uint32_t>(rf * 18014398509481984.0f)) << 32;
+    const uint64_t B = mb << 10;  // b_m * 2^62
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        const int64_t e = static_cast<int64_t>(0x2000000000000000ULL - wr_umulhi(B, Y));  // (1 - b y) * 2^61
+        const uint64_t c = e >= 0 ? wr_umulhi(Y, static_cast<uint64_t>(e)) : 0 - wr_umulhi(Y, static_cast<uint64_t>(-e));
+        Y += c << 3;
+    }
+    // Q ~ floor(ma * 2^(53+adj) / mb), exact remainder R
+    uint64_t Q = wr_umulhi(ma << (2 + adj), Y);
+    int64_t R = static_cast<int64_t>((ma << (53 + adj)) - Q * mb);
+    const int64_t smb = static_cast<int64_t>(mb);
+    if (R < 0) { Q -= 1; R += smb; }
+    if (R < 0) { Q -= 1; R += smb; }
+    if (R >= smb) { Q += 1; R -= smb; }
+    if (R >= smb) { Q += 1; R -= smb; }
+    uint64_t mant = Q >> 1;
+    const bool up = (Q & 1) && (R != 0 || (mant & 1));
+    mant += up ? 1 : 0;
+    int e2 = be;
+    if (mant >> 53) {
+        mant >>= 1;
+        e2 += 1;
+        if (e2 > 2046) return a / b;
+    }
+    return wr_from_bits(((ua ^ ub) & 0x8000000000000000ULL) | (static_cast<uint64_t>(e2) << 52) |
+                        (mant & 0x000fffffffffffffULL));
+}
+
 WR_MHD double wr_exp(double x) {
     const uint64_t u = wr_bits(x);
     const uint64_t ax = u & 0x7fffffffffffffffULL;
@@ -283,7 +337,7 @@ WR_MHD double wr_cbrt(double x) {
     const uint64_t b = wr_bits(a);
     double y = wr_from_bits(b / 3 + 0x2a9f800000000000ULL);
     const double third = 1.0 / 3.0;
-    for (int it = 0; it < 4; ++it) y = y + (a / (y * y) - y) * third;
+    for (int it = 0; it < 4; ++it) y = y + (wr_div_int(a, y * y) - y) * third;
     y = y * scale;
     return (u >> 63) ? -y : y;
 }

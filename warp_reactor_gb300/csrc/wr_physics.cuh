@@ -14,6 +14,11 @@
 
 namespace wr {
 
+// Division on the device: the IEEE quotient computed on the integer pipe
+// (wr_div_int), one shared out-of-line copy.  Bit-identical to a / b.
+static __device__ __noinline__ double wr_div_call(double a, double b) { return wr_div_int(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return wr_div_call(a, b); }
+
 constexpr int NS = 14;
 constexpr int NEQ = 15;
 
@@ -85,10 +90,10 @@ __device__ __forceinline__ Eos eos_sums(const double* xn) {
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
         sa += xn[n];
-        sg += (xn[n] * kMp / rhotot) * inv_gm1(n);
+        sg += ddiv(xn[n] * kMp, rhotot) * inv_gm1(n);
     }
-    sa *= kMp / rhotot;
-    sg /= sa;
+    sa *= ddiv(kMp, rhotot);
+    sg = ddiv(sg, sa);
     return {sa, sg};
 }
 // eos_rt: e from T, reproducer.cpp:306-309
@@ -99,7 +104,7 @@ __device__ __forceinline__ double eos_e_from_T(const double* xn, double T) {
 // eos_re: T from e, reproducer.cpp:311-314
 __device__ __forceinline__ double eos_T_from_e(const double* xn, double e) {
     const Eos q = eos_sums(xn);
-    return e / (q.sum_gammasinv * kGasConstant * q.sum_abarinv);
+    return ddiv(e, q.sum_gammasinv * kGasConstant * q.sum_abarinv);
 }
 
 // balance_charge, reproducer.cpp:316-319
@@ -114,13 +119,13 @@ __device__ __forceinline__ void floor_and_normalize(double* xn, double rho) {
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
         xn[n] = smax(xn[n], kFloor);
-        mf[n] = mass(n) * xn[n] / rho;
+        mf[n] = ddiv(mass(n) * xn[n], rho);
         sum += mf[n];
     }
 #pragma unroll
     for (int n = 0; n < NS; ++n) {
-        mf[n] /= sum;
-        xn[n] = mf[n] * rho / mass(n);
+        mf[n] = ddiv(mf[n], sum);
+        xn[n] = ddiv(mf[n] * rho, mass(n));
     }
 }
 
@@ -150,7 +155,7 @@ __host__ __device__ __forceinline__ double perturbation_factor(int cell, int ste
 __device__ __forceinline__ double collapse_timestep(const double* xn) {
     const double rho = density(xn);
     if (!valid_positive(rho)) return -1.0;
-    const double tff = sqrt(kPi * 3.0 / (32.0 * rho * kGrav));
+    const double tff = sqrt(ddiv(kPi * 3.0, 32.0 * rho * kGrav));
     if (!valid_positive(tff)) return -1.0;
     const double dt = kTffReduc * tff;
     return valid_positive(dt) ? dt : -1.0;
