@@ -143,6 +143,14 @@ typedef struct wr_run_timing {
 } wr_run_timing;
 
 int wr_set_profiling(wr_ctx* ctx, int on);
+
+/* Launch shape of the advance kernel (the knob the autotuner sweeps):
+ *   0  128 lanes per SM, per-lane iteration matrix in shared memory
+ *   1  256 lanes per SM (2 blocks of 128), iteration matrix in global memory
+ *   2  256 lanes per SM (1 block of 256), iteration matrix in global memory
+ * Results are identical for every variant; only the speed differs.  No reference
+ * counterpart (the reference fixes 128 threads per block, reproducer.cpp:7398). */
+int wr_set_advance_variant(wr_ctx* ctx, int variant);
 int wr_get_run_timing(wr_ctx* ctx, wr_run_timing* out);
 
 /* Drop-in for run_cells_cuda (reproducer.cpp:7791-7975): create, upload, run,

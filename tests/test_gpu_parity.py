@@ -52,8 +52,7 @@ def test_network_portable_bitwise(wr, gpu, oracle_port):
         Jo, fo = oracle_port.net_jac(X[i], T[i])
         assert same(J[i], Jo), i
         assert same(f[i], fo), i
-    g_ok = np.isfinite(J[: len(g["T"])]).all()
-    assert g_ok  # the reference's own fixture states are all finite
+
 
 
 def test_network_cuda_math_close_to_reference(wr, gpu):
@@ -197,3 +196,18 @@ def test_full_grid_64_replay_sample(wr, gpu, oracle_port):
     assert np.isfinite(cells["T"]).all() and (cells["xn"] > 0).all()
     live = cells["completed_steps"] == cgs
     assert (cells["time"][live] == cells["time"][live][0]).all()
+
+
+@pytest.mark.parametrize("variant", [1, 2])
+def test_advance_variants_identical(wr, gpu, variant):
+    """Every launch shape of the advance kernel gives the same bits."""
+    a = wr.make_grid(3)
+    rc0, cgs0 = wr.run_cells(a, True)
+    b = wr.make_grid(3)
+    with wr.Context(len(b)) as ctx:
+        ctx.set_variant(variant)
+        ctx.upload(b)
+        rc, cgs = ctx.run(True)
+        ctx.download(b)
+    assert rc == rc0 == wr.SUCCESS and cgs == cgs0
+    assert a.tobytes() == b.tobytes()

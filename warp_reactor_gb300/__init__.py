@@ -92,6 +92,7 @@ def lib() -> ctypes.CDLL:
         L.wr_make_collapse_state.argtypes = [vp]
         L.wr_make_collapse_state.restype = None
         L.wr_set_profiling.argtypes = [vp, ctypes.c_int]
+        L.wr_set_advance_variant.argtypes = [vp, ctypes.c_int]
         L.wr_get_run_timing.argtypes = [vp, ctypes.POINTER(RunTiming)]
         L.wr_dt_history.argtypes = [vp, vp, ctypes.c_int]
         L.wr_diag_fp64_peak.argtypes = [dp]
@@ -179,6 +180,12 @@ class Context:
         cnt = ctypes.c_int()
         rc = lib().wr_advance(self.handle, completed_global_steps, next_grid_time, dt_grid, ctypes.byref(cnt))
         return rc, cnt.value
+
+    def set_variant(self, variant: int) -> None:
+        """Advance-kernel launch shape (0, 1, 2); results do not depend on it."""
+        rc = lib().wr_set_advance_variant(self.handle, int(variant))
+        if rc != SUCCESS:
+            raise WarpReactorError(rc, f"wr_set_advance_variant ({last_error()})")
 
     def set_profiling(self, on: bool = True) -> None:
         rc = lib().wr_set_profiling(self.handle, int(bool(on)))

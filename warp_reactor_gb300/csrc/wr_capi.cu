@@ -44,12 +44,15 @@ struct wr_ctx {
     int device = 0;
     int math = WR_MATH_PORTABLE;
     int advance_blocks = 0;
+    int sms = 1;
+    int variant = 0;
     cudaStream_t stream = nullptr;
     DevState s{};
     void* state_buf = nullptr;
     StepCtl* ctl = nullptr;
     StepCtl* host_ctl = nullptr;  // pinned mirror
     double* jbackup = nullptr;
+    double* ebuf = nullptr;    // per-lane iteration matrices for the global-matrix variants
     double* dt_hist = nullptr;  // grid dt of every outer step of the last wr_run
     wr_collapse_state* staging = nullptr;  // device AoS records for upload/download
     // optional per-kernel timing of wr_run (CUDA events on the context stream)
@@ -105,8 +108,19 @@ __global__ void k_pack(DevState s, wr_collapse_state* __restrict__ out) {
     out[i] = c;
 }
 
+// scatter the queued cells (those whose completed steps equal the grid's) into
+// the bucket order
+__global__ void k_order(DevState s, StepCtl* ctl) {
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= s.n || ctl->stop) return;
+    if (s.steps[cell] != ctl->cgs) return;
+    const unsigned int pos = atomicAdd(&ctl->off[cost_bucket(s.cost[cell])], 1u);
+    if (pos < static_cast<unsigned int>(s.n)) s.order[pos] = cell;
+}
+
 // start of an outer step driven by the host (wr_prepare)
 __global__ void k_begin_step(StepCtl* ctl, int cgs, double grid_time, int step, int perturb) {
+    for (int b = 0; b < kBuckets; ++b) ctl->hist[b] = 0;
     ctl->cgs = cgs;
     ctl->grid_time = grid_time;
     ctl->step = step;
@@ -121,8 +135,8 @@ __global__ void k_begin_advance(StepCtl* ctl, int cgs, double next_grid_time, do
     ctl->next_grid_time = next_grid_time;
     ctl->dt_grid = dt_grid;
     ctl->integrated = 0;
-    ctl->queue = 0;
     ctl->stop = 0;
+    build_queue_offsets(ctl);
 }
 
 // host checks between prepare and advance, reproducer.cpp:7880-7909
@@ -146,7 +160,7 @@ __global__ void k_decide(StepCtl* ctl, double* dt_hist) {
     ctl->dt_grid = dt;
     ctl->next_grid_time = next;
     ctl->integrated = 0;
-    ctl->queue = 0;
+    build_queue_offsets(ctl);
     if (ctl->step >= 0 && ctl->step < WR_MAX_COLLAPSE_STEPS) dt_hist[ctl->step] = dt;
 }
 
@@ -179,9 +193,16 @@ void record(wr_ctx* ctx, int idx) {
 
 cudaError_t launch_advance(wr_ctx* ctx) {
     g_launches.fetch_add(1, std::memory_order_relaxed);
+    const int blocks = ctx->sms * kAdvanceShapes[ctx->variant].blocks_per_sm;
     if (ctx->math == WR_MATH_CUDA)
-        return launch_advance_cuda(ctx->advance_blocks, ctx->stream, ctx->s, ctx->ctl, ctx->jbackup);
-    return launch_advance_portable(ctx->advance_blocks, ctx->stream, ctx->s, ctx->ctl, ctx->jbackup);
+        return launch_advance_cuda(ctx->variant, blocks, ctx->stream, ctx->s, ctx->ctl, ctx->jbackup, ctx->ebuf);
+    return launch_advance_portable(ctx->variant, blocks, ctx->stream, ctx->s, ctx->ctl, ctx->jbackup, ctx->ebuf);
+}
+
+cudaError_t launch_order(wr_ctx* ctx) {
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    k_order<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->s, ctx->ctl);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_prepare(wr_ctx* ctx) {
@@ -228,14 +249,20 @@ int wr_create(int num_cells, int device, int math_mode, wr_ctx** out) {
         return fail("cudaStreamCreate", e);
     }
     const size_t n = static_cast<size_t>(num_cells);
-    const size_t bytes = n * sizeof(double) * (3 + NS + 2) + n * sizeof(uint64_t) * 7 + n * sizeof(int);
+    const size_t bytes = n * sizeof(double) * (3 + NS + 2) + n * sizeof(uint64_t) * 7 + n * sizeof(int) * 3;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    ctx->advance_blocks = sms > 0 ? sms : 1;
-    const size_t nslots = static_cast<size_t>(ctx->advance_blocks) * kAdvanceThreads;
+    ctx->sms = sms > 0 ? sms : 1;
+    ctx->advance_blocks = ctx->sms;
+    size_t nslots = 0;  // lane slots of the largest configuration
+    for (const AdvanceShape& sh : kAdvanceShapes) {
+        const size_t slots = static_cast<size_t>(ctx->sms) * sh.blocks_per_sm * sh.threads;
+        nslots = slots > nslots ? slots : nslots;
+    }
     e = cudaMalloc(&ctx->state_buf, bytes);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->ctl, sizeof(StepCtl));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->jbackup, nslots * NEQ * NEQ * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->ebuf, nslots * NEQ * NEQ * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->dt_hist, WR_MAX_COLLAPSE_STEPS * sizeof(double));
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->host_ctl, sizeof(StepCtl));
     if (e == cudaSuccess) e = ctx->math == WR_MATH_CUDA ? configure_advance_cuda() : configure_advance_portable();
@@ -258,6 +285,8 @@ int wr_create(int num_cells, int device, int math_mode, wr_ctx** out) {
     ctx->s.time = reinterpret_cast<double*>(take(n * sizeof(double)));
     ctx->s.driver = reinterpret_cast<double*>(take(n * sizeof(double)));
     ctx->s.steps = reinterpret_cast<int*>(take(n * sizeof(int)));
+    ctx->s.cost = reinterpret_cast<int*>(take(n * sizeof(int)));
+    ctx->s.order = reinterpret_cast<int*>(take(n * sizeof(int)));
     StepCtl init{};
     init.dmin_bits = kDblMaxBits;
     init.failure = WR_SUCCESS;
@@ -279,6 +308,7 @@ void wr_destroy(wr_ctx* ctx) {
     cudaFree(ctx->state_buf);
     cudaFree(ctx->ctl);
     cudaFree(ctx->jbackup);
+    cudaFree(ctx->ebuf);
     cudaFree(ctx->dt_hist);
     cudaFree(ctx->staging);
     cudaFreeHost(ctx->host_ctl);
@@ -302,6 +332,8 @@ int wr_upload(wr_ctx* ctx, const wr_collapse_state* cells) {
     if (e != cudaSuccess) return fail("cudaMemcpyAsync(cells to device)", e);
     g_launches.fetch_add(1, std::memory_order_relaxed);
     k_unpack<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->staging, ctx->s);
+    e = cudaMemsetAsync(ctx->s.cost, 0, static_cast<size_t>(ctx->n) * sizeof(int), ctx->stream);
+    if (e != cudaSuccess) return fail("cudaMemsetAsync(cost)", e);
     StepCtl init{};
     init.dmin_bits = kDblMaxBits;
     init.failure = WR_SUCCESS;
@@ -347,7 +379,8 @@ int wr_advance(wr_ctx* ctx, int completed_global_steps, double next_grid_time, d
     if (rc != WR_SUCCESS) return rc;
     g_launches.fetch_add(1, std::memory_order_relaxed);
     k_begin_advance<<<1, 1, 0, ctx->stream>>>(ctx->ctl, completed_global_steps, next_grid_time, dt_grid);
-    cudaError_t e = launch_advance(ctx);
+    cudaError_t e = launch_order(ctx);
+    if (e == cudaSuccess) e = launch_advance(ctx);
     if (e != cudaSuccess) return fail("advance launch", e);
     rc = read_ctl(ctx);
     if (rc != WR_SUCCESS) return rc;
@@ -372,8 +405,9 @@ int wr_run(wr_ctx* ctx, int perturb, int* completed_global_steps) {
         if (e == cudaSuccess) {
             g_launches.fetch_add(1, std::memory_order_relaxed);
             k_decide<<<1, 1, 0, ctx->stream>>>(ctx->ctl, ctx->dt_hist);
+            e = launch_order(ctx);
             record(ctx, 4 * step + 2);
-            e = launch_advance(ctx);
+            if (e == cudaSuccess) e = launch_advance(ctx);
             record(ctx, 4 * step + 3);
         }
         steps_launched = step + 1;
@@ -410,6 +444,13 @@ int wr_run(wr_ctx* ctx, int perturb, int* completed_global_steps) {
     }
     *completed_global_steps = ctx->host_ctl->cgs;
     return ctx->host_ctl->failure;
+}
+
+int wr_set_advance_variant(wr_ctx* ctx, int variant) {
+    if (!ctx) return fail_msg("wr_set_advance_variant: null context");
+    if (variant < 0 || variant >= kAdvanceVariants) return fail_msg("wr_set_advance_variant: unknown variant");
+    ctx->variant = variant;
+    return WR_SUCCESS;
 }
 
 int wr_set_profiling(wr_ctx* ctx, int on) {

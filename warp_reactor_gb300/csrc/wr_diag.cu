@@ -49,11 +49,11 @@ __global__ void k_diag_lu(int n, const double* __restrict__ A, const double* __r
 #pragma unroll
         for (int c = 0; c < NEQ; ++c) E(r, c) = A[static_cast<size_t>(i) * NEQ * NEQ + r * NEQ + c];
     int ip[NEQ];
-    const int inf = lu_decompose<kLuThreads>(E, ip);
+    const int inf = lu_decompose(E, ip);
     double v[NEQ];
 #pragma unroll
     for (int k = 0; k < NEQ; ++k) v[k] = b[i * NEQ + k];
-    if (inf == 0) lu_solve<kLuThreads>(E, ip, v);
+    if (inf == 0) lu_solve(E, ip, v);
 #pragma unroll
     for (int r = 0; r < NEQ; ++r)
 #pragma unroll

@@ -26,6 +26,7 @@
 
 #include <cfloat>
 #include <stdint.h>
+#include <type_traits>
 
 #include "../../include/warp_reactor.h"
 #include "wr_physics.cuh"
@@ -46,8 +47,18 @@ struct DevState {
     double* driver;
     int* steps;
     uint64_t* stats;  // [7][n]
+    int* cost;        // ROS2S attempts of the cell's last burn (scheduling hint)
+    int* order;       // advance work queue: cells of this step, heaviest first
     int n;
 };
+
+// Work-queue order: cells are bucketed by last step's attempt count, heaviest
+// bucket first (longest-processing-time-first list scheduling), so the cells that
+// set a step's length start early instead of straggling at the end.
+constexpr int kBuckets = 64;
+__host__ __device__ __forceinline__ int cost_bucket(int cost) {
+    return kBuckets - 1 - (cost < kBuckets - 1 ? (cost > 0 ? cost : 0) : kBuckets - 1);
+}
 
 struct StepCtl {
     unsigned long long dmin_bits;  // grid minimum of the candidates (double bits)
@@ -61,7 +72,9 @@ struct StepCtl {
     double dt_grid;
     double next_grid_time;
     unsigned int queue;            // work-queue head of k_advance
-    unsigned int pad_;
+    unsigned int queued;           // cells in the work queue of this step
+    unsigned int hist[kBuckets];   // queued cells per cost bucket (k_prepare)
+    unsigned int off[kBuckets];    // bucket start offsets in `order`
 };
 
 constexpr unsigned long long kDblMaxBits = 0x7fefffffffffffffULL;
@@ -108,6 +121,9 @@ __device__ __forceinline__ void record_failure(StepCtl* ctl, int code) {
 template <int B>
 __global__ void __launch_bounds__(B) k_prepare(DevState s, StepCtl* ctl) {
     __shared__ unsigned long long red[B / 32];
+    __shared__ unsigned int hist[kBuckets];
+    for (int i = threadIdx.x; i < kBuckets; i += B) hist[i] = 0;
+    __syncthreads();
     const int stop = ctl->stop;
     const int cgs = ctl->cgs;
     const double grid_time = ctl->grid_time;
@@ -151,6 +167,7 @@ __global__ void __launch_bounds__(B) k_prepare(DevState s, StepCtl* ctl) {
                     cand = static_cast<unsigned long long>(__double_as_longlong(dt));
                 }
                 s.driver[cell] = driver;
+                atomicAdd(&hist[cost_bucket(s.cost[cell])], 1u);
             }
         }
     }
@@ -168,23 +185,48 @@ __global__ void __launch_bounds__(B) k_prepare(DevState s, StepCtl* ctl) {
         for (int w = 1; w < B / 32; ++w) m = red[w] < m ? red[w] : m;
         if (m != kDblMaxBits) atomicMin(&ctl->dmin_bits, m);
     }
+    for (int i = threadIdx.x; i < kBuckets; i += B)
+        if (hist[i]) atomicAdd(&ctl->hist[i], hist[i]);
+}
+
+// bucket offsets from the histogram (one thread), resetting the histogram
+__device__ __forceinline__ void build_queue_offsets(StepCtl* ctl) {
+    unsigned int acc = 0;
+    for (int b = 0; b < kBuckets; ++b) {
+        ctl->off[b] = acc;
+        acc += ctl->hist[b];
+        ctl->hist[b] = 0;
+    }
+    ctl->queued = acc;
+    ctl->queue = 0;
 }
 
 
+
+
 // ------------------------------------------------------------------ advance
-// Per-lane matrix storage in shared memory: element (r, c) of lane l at
-// smem[(r*15 + c) * B + l]; 32 consecutive lanes touch 32 consecutive doubles.
+// Per-lane 15x15 matrix storage: element (r, c) of lane l at base[(r*15 + c) * stride]
+// with base pointing at the lane's first element, so 32 consecutive lanes touch 32
+// consecutive doubles.  Shared memory (stride = threads per block, a compile-time
+// constant) or a global per-lane slot array (stride = number of lane slots).
 template <int B>
 struct Mat {
     double* base;
     __device__ __forceinline__ double& operator()(int r, int c) const { return base[(r * NEQ + c) * B]; }
+    __device__ __forceinline__ double& at(int idx) const { return base[idx * B]; }
+};
+struct MatG {
+    double* base;
+    int stride;
+    __device__ __forceinline__ double& operator()(int r, int c) const { return base[(r * NEQ + c) * stride]; }
+    __device__ __forceinline__ double& at(int idx) const { return base[idx * stride]; }
 };
 
-// J sink of the generated network: E = -J into shared memory, J into the lane's
+// J sink of the generated network: E = -J into the lane's matrix, J into the lane's
 // global backup (re-read only when an attempt is retried with the same J)
-template <int B>
+template <class MT>
 struct JSink {
-    Mat<B> E;
+    MT E;
     double* jb;
     int stride;
     __device__ __forceinline__ void operator()(int r, int c, double v) {
@@ -202,8 +244,8 @@ __device__ __forceinline__ void state_from_y(const double* y, double* X, double&
 
 // lu_decomposition<15> (reproducer.cpp:96-151) on the lane's shared-memory matrix.
 // Row interchanges move whole rows; pivot indices are returned in ip.
-template <int B>
-__device__ __forceinline__ int lu_decompose(Mat<B> A, int* ip) {
+template <class MT>
+__device__ __forceinline__ int lu_decompose(MT A, int* ip) {
     int info = 0;
 #pragma unroll
     for (int k = 0; k < NEQ - 1; ++k) {
@@ -218,15 +260,15 @@ __device__ __forceinline__ int lu_decompose(Mat<B> A, int* ip) {
             }
         }
         ip[k] = p;
-        const double apk = A.base[(p * NEQ + k) * B];
+        const double apk = A.at(p * NEQ + k);
         if (apk != 0.0) {
             if (p != k) {
-                A.base[(p * NEQ + k) * B] = A(k, k);
+                A.at(p * NEQ + k) = A(k, k);
                 A(k, k) = apk;
 #pragma unroll
                 for (int j = k + 1; j < NEQ; ++j) {
-                    const double tr = A.base[(p * NEQ + j) * B];
-                    A.base[(p * NEQ + j) * B] = A(k, j);
+                    const double tr = A.at(p * NEQ + j);
+                    A.at(p * NEQ + j) = A(k, j);
                     A(k, j) = tr;
                 }
             }
@@ -254,8 +296,8 @@ __device__ __forceinline__ int lu_decompose(Mat<B> A, int* ip) {
 
 // lu_solve<15> (reproducer.cpp:154-181); x stays in registers, the pivot swap is a
 // select chain instead of a dynamically indexed register array
-template <int B>
-__device__ __forceinline__ void lu_solve(Mat<B> LU, const int* ip, double* x) {
+template <class MT>
+__device__ __forceinline__ void lu_solve(MT LU, const int* ip, double* x) {
 #pragma unroll
     for (int k = 0; k < NEQ - 1; ++k) {
         const int p = ip[k];
@@ -287,17 +329,29 @@ struct Lane {
     bool reject, last, fresh;
 };
 
-template <class M, int B>
-__global__ void __launch_bounds__(B, 1) k_advance(DevState s, StepCtl* ctl, double* __restrict__ jbackup) {
+// Advance kernel configurations (lane slots = blocks x B):
+//   B threads per block, MINB resident blocks per SM (register budget), SMEM_E
+//   whether the per-lane iteration matrix lives in shared memory (225 doubles per
+//   lane) or in the global per-lane array `ebuf`.
+template <class M, int B, int MINB, bool SMEM_E>
+__global__ void __launch_bounds__(B, MINB) k_advance(DevState s, StepCtl* ctl, double* __restrict__ jbackup,
+                                                   double* __restrict__ ebuf) {
     extern __shared__ double smem[];
+    using MT = typename std::conditional<SMEM_E, Mat<B>, MatG>::type;
     if (ctl->stop) return;
     const int n = s.n;
     const int cgs = ctl->cgs;
     const double dt_grid = ctl->dt_grid;
     const double next_grid_time = ctl->next_grid_time;
+    const unsigned int queued = ctl->queued;
     const int lane_slot = blockIdx.x * B + threadIdx.x;
     const int nslots = gridDim.x * B;
-    Mat<B> E{smem + threadIdx.x};
+    MT E;
+    if constexpr (SMEM_E) {
+        E = MT{smem + threadIdx.x};
+    } else {
+        E = MT{ebuf + lane_slot, nslots};
+    }
     double* jb = jbackup + lane_slot;
 
     Lane L;
@@ -313,10 +367,12 @@ __global__ void __launch_bounds__(B, 1) k_advance(DevState s, StepCtl* ctl, doub
         while (alive) {
             if (!have) {
                 if (ctl->failure != WR_SUCCESS) { alive = false; break; }
-                cell = static_cast<int>(atomicAdd(&ctl->queue, 1u));
-                if (cell >= n) { alive = false; break; }
+                const unsigned int q = atomicAdd(&ctl->queue, 1u);
+                if (q >= queued) { alive = false; break; }
+                cell = s.order[q];
                 // advance_collapse_gridwide_kernel prologue, reproducer.cpp:7748-7768
                 if (s.steps[cell] != cgs) continue;
+                s.cost[cell] = 0;
                 double xn[NS];
 #pragma unroll
                 for (int k = 0; k < NS; ++k) xn[k] = s.xn[k * n + cell];
@@ -377,6 +433,7 @@ __global__ void __launch_bounds__(B, 1) k_advance(DevState s, StepCtl* ctl, doub
                     static_cast<uint64_t>(L.n_reject)};
 #pragma unroll
                 for (int k = 0; k < 7; ++k) s.stats[k * n + cell] += st[k];
+                s.cost[cell] = L.n_step;
                 if (code == WR_SUCCESS) {
                     double xn[NS];
 #pragma unroll
@@ -407,7 +464,7 @@ __global__ void __launch_bounds__(B, 1) k_advance(DevState s, StepCtl* ctl, doub
         if (alive && have && L.fresh) {
             double X[NS], T;
             state_from_y(y, X, T);
-            JSink<B> sink{E, jb, nslots};
+            JSink<MT> sink{E, jb, nslots};
             wr_net_jac_rhs<M>(X, T, f0, sink);
             L.n_jac += 1;
             L.fresh = false;
@@ -424,7 +481,7 @@ __global__ void __launch_bounds__(B, 1) k_advance(DevState s, StepCtl* ctl, doub
             const double fac = ddiv(1.0, h * kGamma);
 #pragma unroll
             for (int i = 0; i < NEQ; ++i) E(i, i) = E(i, i) + fac;
-            const int info = lu_decompose<B>(E, ip);
+            const int info = lu_decompose(E, ip);
             if (info != 0) {
                 L.nsing += 1;
                 if (L.nsing >= 5) {
@@ -448,7 +505,7 @@ __global__ void __launch_bounds__(B, 1) k_advance(DevState s, StepCtl* ctl, doub
                 double ak1[NEQ], ak2[NEQ], w[NEQ];
 #pragma unroll
                 for (int i = 0; i < NEQ; ++i) ak1[i] = f0[i];
-                lu_solve<B>(E, ip, ak1);
+                lu_solve(E, ip, ak1);
                 // stages 2 and 3 share one inlined RHS evaluation
 #pragma unroll 1
                 for (int stage = 2; stage <= 3; ++stage) {
@@ -471,7 +528,7 @@ __global__ void __launch_bounds__(B, 1) k_advance(DevState s, StepCtl* ctl, doub
                     wr_net_rhs<M>(X, T, dy);
 #pragma unroll
                     for (int i = 0; i < NEQ; ++i) w[i] += dy[i];
-                    lu_solve<B>(E, ip, w);
+                    lu_solve(E, ip, w);
                     if (stage == 2) {
 #pragma unroll
                         for (int i = 0; i < NEQ; ++i) ak2[i] = w[i];

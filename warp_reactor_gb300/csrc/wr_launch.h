@@ -9,14 +9,30 @@
 
 namespace wr {
 
-constexpr int kAdvanceThreads = 128;  // one warp per SM sub-partition
 constexpr int kPrepareThreads = 256;
 
-// dynamic shared memory of k_advance: one 15x15 FP64 matrix per lane
-constexpr size_t advance_smem_bytes(int threads) { return static_cast<size_t>(NEQ) * NEQ * threads * sizeof(double); }
+// Advance kernel configurations, selected per context (wr_set_advance_variant):
+//   0  128 threads x 1 block per SM, iteration matrix in shared memory (225 KiB)
+//   1  128 threads x 2 blocks per SM, iteration matrix in a global lane array
+//   2  256 threads x 1 block per SM, iteration matrix in a global lane array
+constexpr int kAdvanceVariants = 3;
+struct AdvanceShape {
+    int threads;
+    int blocks_per_sm;
+    bool smem_matrix;
+};
+constexpr AdvanceShape kAdvanceShapes[kAdvanceVariants] = {{128, 1, true}, {128, 2, false}, {256, 1, false}};
 
-cudaError_t launch_advance_portable(int blocks, cudaStream_t stream, DevState s, StepCtl* ctl, double* jbackup);
-cudaError_t launch_advance_cuda(int blocks, cudaStream_t stream, DevState s, StepCtl* ctl, double* jbackup);
+constexpr size_t advance_smem_bytes(int variant) {
+    return kAdvanceShapes[variant].smem_matrix
+               ? static_cast<size_t>(NEQ) * NEQ * kAdvanceShapes[variant].threads * sizeof(double)
+               : 0;
+}
+
+cudaError_t launch_advance_portable(int variant, int blocks, cudaStream_t stream, DevState s, StepCtl* ctl,
+                                    double* jbackup, double* ebuf);
+cudaError_t launch_advance_cuda(int variant, int blocks, cudaStream_t stream, DevState s, StepCtl* ctl,
+                                double* jbackup, double* ebuf);
 cudaError_t configure_advance_portable();
 cudaError_t configure_advance_cuda();
 
