@@ -48,7 +48,7 @@ __global__ void k_diag_lu(int n, const double* __restrict__ A, const double* __r
     for (int r = 0; r < NEQ; ++r)
 #pragma unroll
         for (int c = 0; c < NEQ; ++c) E(r, c) = A[static_cast<size_t>(i) * NEQ * NEQ + r * NEQ + c];
-    int ip[NEQ];
+    uint64_t ip = 0;
     const int inf = lu_decompose(E, ip);
     double v[NEQ];
 #pragma unroll
@@ -60,7 +60,7 @@ __global__ void k_diag_lu(int n, const double* __restrict__ A, const double* __r
         for (int c = 0; c < NEQ; ++c) LU[static_cast<size_t>(i) * NEQ * NEQ + r * NEQ + c] = E(r, c);
 #pragma unroll
     for (int k = 0; k < NEQ; ++k) {
-        ipvt[i * NEQ + k] = ip[k];
+        ipvt[i * NEQ + k] = static_cast<int>((ip >> (4 * k)) & 15);
         x[i * NEQ + k] = v[k];
     }
     info[i] = inf;

@@ -242,16 +242,22 @@ __device__ __forceinline__ void state_from_y(const double* y, double* X, double&
     T = eos_T_from_e(X, y[NS]);
 }
 
-// lu_decomposition<15> (reproducer.cpp:96-151) on the lane's shared-memory matrix.
-// Row interchanges move whole rows; pivot indices are returned in ip.
+// lu_decomposition<15> (reproducer.cpp:96-151) on the lane's matrix: the same
+// pivot rule (first strictly larger |a_ik|), row interchange of columns k..14,
+// negated multipliers and column-oriented update, with the operations in the
+// reference's order.  The loops stay rolled: the matrix is in memory anyway, and
+// a fully unrolled 15x15 elimination is ~20k instructions of code that the
+// instruction cache then has to stream for every attempt.  Pivot indices are
+// returned packed four bits each (ip = pivot row of column k at bits 4k..4k+3).
 template <class MT>
-__device__ __forceinline__ int lu_decompose(MT A, int* ip) {
+__device__ __forceinline__ int lu_decompose(MT A, uint64_t& ip) {
     int info = 0;
-#pragma unroll
+    uint64_t piv = 0;
+#pragma unroll 1
     for (int k = 0; k < NEQ - 1; ++k) {
         int p = k;
         double maxv = ::fabs(A(k, k));
-#pragma unroll
+#pragma unroll 1
         for (int i = k + 1; i < NEQ; ++i) {
             const double v = ::fabs(A(i, k));
             if (v > maxv) {
@@ -259,48 +265,42 @@ __device__ __forceinline__ int lu_decompose(MT A, int* ip) {
                 p = i;
             }
         }
-        ip[k] = p;
-        const double apk = A.at(p * NEQ + k);
-        if (apk != 0.0) {
+        piv |= static_cast<uint64_t>(p) << (4 * k);
+        if (A(p, k) != 0.0) {
             if (p != k) {
-                A.at(p * NEQ + k) = A(k, k);
-                A(k, k) = apk;
-#pragma unroll
-                for (int j = k + 1; j < NEQ; ++j) {
-                    const double tr = A.at(p * NEQ + j);
-                    A.at(p * NEQ + j) = A(k, j);
-                    A(k, j) = tr;
+#pragma unroll 1
+                for (int j = k; j < NEQ; ++j) {
+                    const double t = A(p, j);
+                    A(p, j) = A(k, j);
+                    A(k, j) = t;
                 }
             }
             const double mult = ddiv(-1.0, A(k, k));
-            double l[NEQ];
-#pragma unroll
-            for (int i = k + 1; i < NEQ; ++i) {
-                l[i] = A(i, k) * mult;
-                A(i, k) = l[i];
-            }
-#pragma unroll
+#pragma unroll 1
+            for (int i = k + 1; i < NEQ; ++i) A(i, k) = A(i, k) * mult;
+#pragma unroll 1
             for (int j = k + 1; j < NEQ; ++j) {
                 const double t = A(k, j);
-#pragma unroll
-                for (int i = k + 1; i < NEQ; ++i) A(i, j) = A(i, j) + t * l[i];
+#pragma unroll 4
+                for (int i = k + 1; i < NEQ; ++i) A(i, j) = A(i, j) + t * A(i, k);
             }
         } else {
             info = k + 1;
         }
     }
-    ip[NEQ - 1] = NEQ - 1;
+    piv |= static_cast<uint64_t>(NEQ - 1) << (4 * (NEQ - 1));
     if (A(NEQ - 1, NEQ - 1) == 0.0) info = NEQ;
+    ip = piv;
     return info;
 }
 
 // lu_solve<15> (reproducer.cpp:154-181); x stays in registers, the pivot swap is a
 // select chain instead of a dynamically indexed register array
 template <class MT>
-__device__ __forceinline__ void lu_solve(MT LU, const int* ip, double* x) {
+__device__ __forceinline__ void lu_solve(MT LU, const uint64_t ip, double* x) {
 #pragma unroll
     for (int k = 0; k < NEQ - 1; ++k) {
-        const int p = ip[k];
+        const int p = static_cast<int>((ip >> (4 * k)) & 15);
         double t = x[k];
 #pragma unroll
         for (int i = k + 1; i < NEQ; ++i) t = (p == i) ? x[i] : t;
@@ -359,7 +359,7 @@ __global__ void __launch_bounds__(B, MINB) k_advance(DevState s, StepCtl* ctl, d
     bool alive = true;   // lane may still take cells
     bool have = false;   // lane holds a cell
     double y[NEQ], f0[NEQ];
-    int ip[NEQ];
+    uint64_t ip = 0;
     int integrated = 0;
 
     while (__any_sync(0xffffffffu, alive)) {
