@@ -145,6 +145,35 @@ def algorithmic_ops(cells):
     return nj * f_j + na * f_att, {"F_J": f_j, "F_RHS": f_rhs, "F_attempt": f_att, "jacobians": nj, "attempts": na}
 
 
+def precision_form(wr, cells0, fp64_cells, device, math_mode):
+    """The precision form (advance variant 3: FP32 factorisation + one FP64 residual
+    refinement per stage solve) on the same grid: device time, and its final-state
+    error against the plain FP64 run (which equals the FP64 oracle bit for bit)."""
+    c = cells0.copy()
+    with wr.Context(len(c), device, math_mode) as ctx:
+        ctx.set_variant(3)
+        ctx.set_profiling(True)
+        ctx.upload(c)
+        rc, cgs = ctx.run(True)
+        t = ctx.run_timing()
+        ctx.download(c)
+    ref = fp64_cells
+    rT = np.abs(c["T"] - ref["T"]) / ref["T"]
+    big = ref["xn"] > 1e-20
+    rx = np.abs(c["xn"] - ref["xn"])[big] / ref["xn"][big]
+    st, rs = c["stats"], ref["stats"]
+    return {
+        "result": int(rc), "cells_per_s": len(c) / (t.run_ms / 1e3), "ms": t.run_ms,
+        "vs_plain_fp64_speedup": None,
+        "T_rel_err_max": float(rT.max()), "T_rel_err_median": float(np.median(rT)),
+        "species_rel_err_max": float(rx.max()), "species_rel_err_median": float(np.median(rx)),
+        "accepted_delta_total": int(st["accepted_steps"].sum()) - int(rs["accepted_steps"].sum()),
+        "rejected_delta_total": int((st["internal_steps"] - st["accepted_steps"]).sum())
+                                - int((rs["internal_steps"] - rs["accepted_steps"]).sum()),
+        "completed_steps_equal": bool((c["completed_steps"] == ref["completed_steps"]).all()),
+    }
+
+
 def cpu_baseline(grid, threads):
     from oracle import oracle
     o = oracle.load("libm")
@@ -242,6 +271,9 @@ def run_gb300(args, rank, ws, local, tdist):
     if rc != wr.SUCCESS:
         raise RuntimeError(f"e2e run failed with {rc}")
     ctx.close()
+    forms = {}
+    if not args.no_forms:
+        forms["precision"] = precision_form(wr, cells0, out, local, math_mode)
     if rank != 0:
         return 0
     cpu = None
@@ -275,10 +307,34 @@ def run_gb300(args, rank, ws, local, tdist):
         "e2e": {"value": ws * n / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": n * 216,
                 "d2h_bytes_per_step": n * 216},
         "gpu_launches": launches,
+        "forms": forms,
         "clocks": clocks.summary(),
         "wall_s_timed": t_wall,
     }
+    if forms.get("precision"):
+        forms["precision"]["vs_plain_fp64_speedup"] = forms["precision"]["cells_per_s"] / (value / ws)
     print(json.dumps(line), flush=True)
+    return 0
+
+
+def probe_fp64():
+    """FP64 issue interval (cycles per FMA per warp) for 1-16 warps on one SM and
+    1/4/8 independent chains per lane, and the whole-GPU FMA rate."""
+    import ctypes
+    import warp_reactor_gb300 as wr
+    from warp_reactor_gb300 import build
+    build.build_all()
+    f = wr.lib().wr_diag_fp64_issue
+    f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    rows = []
+    for warps in (1, 2, 4, 8, 16):
+        row = {"warps_per_sm": warps}
+        for chains in (1, 4, 8):
+            v = ctypes.c_double()
+            assert f(warps, chains, ctypes.byref(v)) == 1
+            row[f"cycles_per_fma_chains{chains}"] = v.value
+        rows.append(row)
+    print(json.dumps({"fp64_issue": rows, "fp64_fma_per_s": wr.fp64_peak()}), flush=True)
     return 0
 
 
@@ -316,9 +372,14 @@ def main():
     ap.add_argument("--cpu-grid", type=int, default=16)
     ap.add_argument("--ref-grid", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the precision-form run")
+    ap.add_argument("--probe-fp64", action="store_true",
+                    help="print this GPU's FP64 issue interval per warp count and the FMA peak, exit")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiling driver: run this many outer steps host-stepped, print nothing, exit")
     args = ap.parse_args()
+    if args.probe_fp64:
+        return probe_fp64()
     if args.profile_steps > 0:
         return profile_steps(args)
     if args.warmup < 3:

@@ -95,6 +95,30 @@ typedef struct wr_ctx wr_ctx;
  * half of run_cells_cuda (reproducer.cpp:7794-7828). */
 int wr_create(int num_cells, int device, int math_mode, wr_ctx** out);
 
+/* A context holding several independent grids batched in one state (the batching
+ * form): grid g owns cells [sum(cells_per_grid[0..g-1]), ... + cells_per_grid[g])
+ * and runs its own gridwide-independent schedule (its own grid minimum, clock,
+ * completed steps and failure code), while one prepare / advance launch covers
+ * every cell of every grid.  Each grid gives the same result as a one-grid
+ * context of its cells.  Host-stepped wr_prepare / wr_advance need one grid; use
+ * wr_run.  No reference counterpart (the reference runs one grid per process). */
+int wr_create_batch(int num_grids, const int* cells_per_grid, int device, int math_mode, wr_ctx** out);
+
+/* Completed global steps and IntegratorResult of one grid after wr_run. */
+int wr_grid_result(wr_ctx* ctx, int grid, int* completed_global_steps, int* result);
+
+/* Grid dt per outer step of one grid of the last wr_run. */
+int wr_grid_dt_history(wr_ctx* ctx, int grid, double* out, int max_steps);
+
+/* Outer-step policy of wr_run.
+ *  WR_POLICY_GRIDWIDE_INDEPENDENT: one grid-wide dt per step, the minimum over
+ *    cells (the reference CUDA program, reproducer.cpp:7696-7785).  Default.
+ *  WR_POLICY_LEGACY_LOCAL: every cell advances with its own free-fall dt (the
+ *    reference CPU program's default, advance_collapse_step, :7646-7685 and the
+ *    loop at :8630-8648); its final_states_grid<N>_cpu.bin is reproduced. */
+enum { WR_POLICY_GRIDWIDE_INDEPENDENT = 0, WR_POLICY_LEGACY_LOCAL = 1 };
+int wr_set_policy(wr_ctx* ctx, int policy);
+
 /* Release every device buffer of the context (reproducer.cpp:7967-7973). */
 void wr_destroy(wr_ctx* ctx);
 
@@ -148,9 +172,18 @@ int wr_set_profiling(wr_ctx* ctx, int on);
  *   0  128 lanes per SM, per-lane iteration matrix in shared memory
  *   1  256 lanes per SM (2 blocks of 128), iteration matrix in global memory
  *   2  256 lanes per SM (1 block of 256), iteration matrix in global memory
- * Results are identical for every variant; only the speed differs.  No reference
+ *   3  the precision form: 256 lanes per SM, the iteration matrix factorised in
+ *      FP32 with one FP64-residual refinement sweep per stage solve; RHS,
+ *      exp/log, stage combination, error norm, controller and EOS stay FP64
+ * Variants 0-2 give identical results (only the speed differs); variant 3
+ * approximates the FP64 result.  No reference
  * counterpart (the reference fixes 128 threads per block, reproducer.cpp:7398). */
 int wr_set_advance_variant(wr_ctx* ctx, int variant);
+
+/* Autotuner: times the first `steps` outer steps of the uploaded state with each
+ * exact launch shape (variants 0-2), restores the state, selects the fastest and
+ * returns it in *best_variant.  The precision form is never chosen by it. */
+int wr_autotune(wr_ctx* ctx, int perturb, int steps, int* best_variant);
 int wr_get_run_timing(wr_ctx* ctx, wr_run_timing* out);
 
 /* Drop-in for run_cells_cuda (reproducer.cpp:7791-7975): create, upload, run,
@@ -161,6 +194,13 @@ int wr_run_cells(wr_collapse_state* cells, int num_cells, int perturb,
 /* The reference's initial collapse cell (make_collapse_state,
  * reproducer.cpp:7533-7546). */
 void wr_make_collapse_state(wr_collapse_state* out);
+
+/* A seeded initial cell of the batching workload (no reference counterpart; the
+ * reference has one initial cell): make_collapse_state with density scaled by
+ * 10^(sigma_dex * N(0,1)) and T log-uniform in [10^log10_tmin, 10^log10_tmax],
+ * e from the EOS.  Deterministic in (grid_id, cell). */
+void wr_make_batch_state(int grid_id, int cell, double sigma_dex, double log10_tmin, double log10_tmax,
+                         wr_collapse_state* out);
 
 /* Text of the last error recorded on this host thread ("" if none). */
 const char* wr_last_error(void);

@@ -48,6 +48,12 @@ int wr_diag_div(int n, const double* a, const double* b, double* out);
  * reference's first launch.  No reference counterpart (benchmark hygiene). */
 int wr_diag_flush_l2(int mib);
 
+/* FP64 issue interval of one warp: one block of `warps` warps on one SM, every lane
+ * running `chains` (1, 4 or 8) independent dependent-FMA chains; returns SM clock
+ * cycles per FMA instruction per warp.  No reference counterpart: the
+ * measurement behind the advance kernel's launch shape. */
+int wr_diag_fp64_issue(int warps, int chains, double* cycles_per_instr);
+
 /* Measured FP64 throughput of this GPU: independent FMA chains in every lane of a
  * full grid, timed with CUDA events.  *dfma_per_s receives FP64 FMA instructions
  * per second per GPU (one FMA = 2 FLOP).  No reference counterpart: the roofline

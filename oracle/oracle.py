@@ -74,6 +74,8 @@ class Oracle:
                        ctypes.POINTER(ctypes.c_int), ctypes.c_int])
         fn("run", [vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_int])
         if kind != "ref":
+            fn("run_legacy", [vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                              ctypes.c_int])
             for name in ("exp", "log", "cbrt"):
                 fn(name, [ctypes.c_double], ctypes.c_double)
         self.lib = L
@@ -95,6 +97,14 @@ class Oracle:
         cgs = ctypes.c_int(completed_global_steps)
         rc = self._f["run"](cells.ctypes.data, len(cells), int(bool(perturb)), ctypes.byref(cgs),
                             int(max_steps), int(nthreads or os.cpu_count() or 1))
+        return rc, cgs.value
+
+    def run_legacy(self, cells, perturb=True, nthreads=None, max_steps=-1):
+        """The reference CPU program's legacy-local loop (reproducer.cpp:8630-8648)."""
+        assert cells.dtype == COLLAPSE_STATE and cells.flags.c_contiguous
+        cgs = ctypes.c_int(0)
+        rc = self._f["run_legacy"](cells.ctypes.data, len(cells), int(bool(perturb)), ctypes.byref(cgs),
+                                   int(max_steps), int(nthreads or os.cpu_count() or 1))
         return rc, cgs.value
 
     def prepare(self, cells, cgs, grid_time, step, perturb=True, nthreads=None):

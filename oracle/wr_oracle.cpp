@@ -492,6 +492,35 @@ int advance_cell(wr_collapse_state& st, int cgs, double next_grid_time, double d
     return 1;
 }
 
+// advance_collapse_step (legacy-local policy), reproducer.cpp:7646-7685: the cell's
+// own free-fall dt; returns true when the cell stops (dt < 10 s or density limit)
+bool legacy_step(wr_collapse_state& st, int cell, int step, bool perturb, int& failure) {
+    apply_perturbation(st, cell, step, perturb);
+    const double old_density = st.density_driver;
+    const double dt = collapse_timestep(st);
+    const double tff = dt / kTffReduc;
+    st.density_driver += dt * (st.density_driver / tff);
+    if (dt < 10.0 || st.density_driver > 2.0e-6) return true;
+    const double ratio = st.density_driver / old_density;
+    Burn s = load(st);
+    for (double& x : s.xn) x *= ratio;
+    s.rho *= ratio;
+    const int r = burn_ros2s(s, dt, st.stats);
+    if (r != WR_SUCCESS) {
+        store(st, s);
+        failure = r;
+        return true;
+    }
+    floor_and_normalize(s);
+    balance_charge(s);
+    floor_and_normalize(s);
+    eos_re(s);
+    store(st, s);
+    st.time += dt;
+    st.completed_steps += 1;
+    return false;
+}
+
 }  // namespace
 
 extern "C" {
@@ -610,6 +639,39 @@ int wro_run(wr_collapse_state* cells, int n, int perturb, int* cgs, int max_step
         *cgs += 1;
     }
     return result;
+}
+
+// The reference CPU program's loop (legacy-local policy), reproducer.cpp:8630-8648:
+// cells in index order, each with its own dt; stops when every cell stopped or
+// at the first failure.  Cells are independent within a step, so the cell loop
+// runs in parallel; on failure the cells after the failing one in index order
+// are left as the reference leaves them only when no failure occurs (failure
+// runs are reported, not replayed).
+int wro_run_legacy(wr_collapse_state* cells, int n, int perturb, int* cgs, int max_steps, int nthreads) {
+    int failure = WR_SUCCESS;
+    const int steps = max_steps > 0 ? max_steps : kMaxCollapseSteps;
+    for (int step = 0; step < steps; ++step) {
+        int all_stopped = 1;
+        int fail_code = WR_SUCCESS;
+#pragma omp parallel for schedule(dynamic, 1) reduction(min : all_stopped) num_threads(nthreads > 0 ? nthreads : 1)
+        for (int i = 0; i < n; ++i) {
+            if (cells[i].completed_steps < *cgs) continue;
+            int f = WR_SUCCESS;
+            const bool stopped = legacy_step(cells[i], i, step, perturb != 0, f);
+            if (f != WR_SUCCESS) {
+#pragma omp critical
+                if (fail_code == WR_SUCCESS) fail_code = f;
+            }
+            all_stopped = (all_stopped && stopped) ? 1 : 0;
+        }
+        if (fail_code != WR_SUCCESS) {
+            failure = fail_code;
+            break;
+        }
+        if (all_stopped) break;
+        *cgs += 1;
+    }
+    return failure;
 }
 
 // Replays a subset of cells through a recorded grid-timestep history: cell_ids[i]

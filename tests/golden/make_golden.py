@@ -18,6 +18,8 @@ Fixtures (all values produced by the reference's own code):
                        run at grid 1, 2, 3, 4 (perturbations on) and grid 2
                        (perturbations off), with the completed global steps
   grid1_stdout_ref.txt the reference CPU program's output for --grid 1
+  legacy_grid{2,3}_ref.bin  final_states_grid<N>_cpu.bin written by the reference
+                       CPU program (its default legacy-local policy) for --grid 2, 3
 """
 import os
 import subprocess
@@ -107,6 +109,13 @@ def main():
     lines = [ln for ln in r.stdout.splitlines() if not ln.startswith("wall time")]
     with open(os.path.join(HERE, "grid1_stdout_ref.txt"), "w") as f:
         f.write("\n".join(lines) + "\n")
+    import shutil
+    import tempfile
+    with tempfile.TemporaryDirectory() as tmp:
+        for g in (2, 3):
+            subprocess.run([exe, "--grid", str(g), "--no-compare-final-state"], capture_output=True, text=True,
+                           check=True, cwd=tmp)
+            shutil.copy(os.path.join(tmp, f"final_states_grid{g}_cpu.bin"), os.path.join(HERE, f"legacy_grid{g}_ref.bin"))
     print("golden fixtures written to", HERE)
 
 

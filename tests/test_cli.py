@@ -79,3 +79,24 @@ def test_grid2_file_rotation_and_compare(exe, gpu, tmp_path, oracle_port, wr):
     # wrong-size file: read error, FAIL
     r = run(exe, "--grid", "2", "--compare-final-state", str(tmp_path / "missing.bin"), cwd=tmp_path)
     assert r.returncode == 1 and "failed to open final-state comparison file" in r.stderr
+
+
+def test_policy_and_write_flags_parse(exe):
+    for bad in (["--driver-policy"], ["--driver-policy", "cta64"], ["--write-final-state"]):
+        r = run(exe, *bad)
+        assert r.returncode == 1 and "usage:" in r.stderr, bad
+
+
+@pytest.mark.gpu
+def test_legacy_local_cli_and_manifest(exe, gpu, tmp_path, oracle_port, wr):
+    out = tmp_path / "legacy.bin"
+    r = run(exe, "--grid", "2", "--driver-policy", "legacy-local", "--write-final-state", str(out), cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert "driver policy: legacy-local" in r.stdout
+    cells = oracle_port.make_grid(2)
+    oracle_port.run_legacy(cells, perturb=True)
+    assert out.read_bytes() == wr.pack_final_states(cells, 2).tobytes()
+    man = (tmp_path / "legacy.bin.manifest").read_text()
+    assert "policy=legacy-local-v1" in man and "cell_count=8" in man
+    r = run(exe, "--grid", "2", "--write-final-state", str(out), cwd=tmp_path)
+    assert r.returncode == 1 and "refusing to overwrite" in r.stderr

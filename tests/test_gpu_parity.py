@@ -211,3 +211,78 @@ def test_advance_variants_identical(wr, gpu, variant):
         ctx.download(b)
     assert rc == rc0 == wr.SUCCESS and cgs == cgs0
     assert a.tobytes() == b.tobytes()
+
+
+def test_precision_form_against_fp64_oracle(wr, gpu, oracle_port):
+    """The precision form (FP32 factorisation + one FP64 residual refinement per
+    stage solve) against the FP64 oracle: same schedule, small final-state error."""
+    grid = 8
+    cells = wr.make_grid(grid)
+    with wr.Context(len(cells)) as ctx:
+        ctx.set_variant(3)
+        ctx.upload(cells)
+        rc, cgs = ctx.run(True)
+        ctx.download(cells)
+    ref = oracle_port.make_grid(grid)
+    rc_o, cgs_o = oracle_port.run(ref, perturb=True)
+    assert rc == rc_o == wr.SUCCESS and cgs == cgs_o
+    assert (cells["completed_steps"] == ref["completed_steps"]).all()
+    rT = np.abs(cells["T"] - ref["T"]) / ref["T"]
+    big = ref["xn"] > 1e-20
+    rx = np.abs(cells["xn"] - ref["xn"])[big] / ref["xn"][big]
+    assert np.median(rT) < 1e-6 and rT.max() < 1e-2
+    assert np.median(rx) < 1e-6
+
+
+def test_batched_grids_equal_separate_runs(wr, gpu, oracle_port):
+    """Batching form: grids of 2^3, 3^3 and 4^3 cells in one context (one launch per
+    kernel for all of them) give, grid by grid, the bits of separate runs; a grid
+    with the batching workload's seeded log-normal density / log-uniform T is
+    checked against the oracle."""
+    sizes = [8, 27, 64, 125]
+    parts = [wr.make_grid(2), wr.make_grid(3), wr.make_grid(4), wr.make_batch_grid(3, 125)]
+    cells = np.concatenate(parts)
+    with wr.Context(grids=sizes) as ctx:
+        ctx.upload(cells)
+        rc, _ = ctx.run(True)
+        results = [ctx.grid_result(g) for g in range(len(sizes))]
+        ctx.download(cells)
+    assert rc == wr.SUCCESS
+    off = 0
+    for g, part in enumerate(parts):
+        ref = part.copy()
+        rc_o, cgs_o = oracle_port.run(ref, perturb=True)
+        assert results[g] == (rc_o, cgs_o)
+        assert cells[off:off + sizes[g]].tobytes() == ref.tobytes(), g
+        off += sizes[g]
+
+
+def test_autotuner_keeps_results(wr, gpu):
+    """The autotuner times the launch shapes on a copy of the state and leaves the
+    state untouched; the run after it gives the same bits as an untuned run."""
+    a = wr.make_grid(3)
+    wr.run_cells(a, True)
+    b = wr.make_grid(3)
+    with wr.Context(len(b)) as ctx:
+        ctx.upload(b)
+        best = ctx.autotune(True, steps=3)
+        assert best in (0, 1, 2)
+        rc, cgs = ctx.run(True)
+        ctx.download(b)
+    assert rc == wr.SUCCESS and a.tobytes() == b.tobytes()
+
+
+@pytest.mark.parametrize("grid", [2, 3])
+def test_legacy_local_policy_bitwise(wr, gpu, oracle_port, grid):
+    """WR_POLICY_LEGACY_LOCAL on the GPU equals the oracle's legacy-local loop (the
+    reference CPU program's default policy) bit for bit."""
+    cells = wr.make_grid(grid)
+    with wr.Context(len(cells)) as ctx:
+        ctx.set_policy(wr.POLICY_LEGACY_LOCAL)
+        ctx.upload(cells)
+        rc, cgs = ctx.run(True)
+        ctx.download(cells)
+    ref = oracle_port.make_grid(grid)
+    rc_o, cgs_o = oracle_port.run_legacy(ref, perturb=True)
+    assert rc == rc_o == wr.SUCCESS and cgs == cgs_o
+    assert cells.tobytes() == ref.tobytes()

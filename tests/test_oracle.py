@@ -149,3 +149,15 @@ def test_partial_sizes_share_exact_output_time(oracle_port, count):
     rc2, n = oracle_port.advance(cells, 0, 0.0 + dt, dt)
     assert rc == rc2 == 1 and n == count
     assert (cells["time"] == dt).all() and (cells["completed_steps"] == 1).all()
+
+
+@pytest.mark.parametrize("grid", [2, 3])
+def test_legacy_local_matches_reference_program(oracle_libm, grid):
+    """The oracle's legacy-local loop (the reference CPU program's default policy)
+    writes the same final_states_grid<N>_cpu.bin as the reference program."""
+    import warp_reactor_gb300 as wr
+    ref = np.fromfile(os.path.join(GOLDEN, f"legacy_grid{grid}_ref.bin"), wr.PACKED_FINAL_STATE)
+    cells = oracle_libm.make_grid(grid)
+    rc, cgs = oracle_libm.run_legacy(cells, perturb=True)
+    assert rc == 1
+    assert wr.pack_final_states(cells, grid).tobytes() == ref.tobytes()

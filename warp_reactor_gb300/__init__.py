@@ -36,6 +36,9 @@ LU_DECOMPOSITION_ERROR = -7
 MATH_PORTABLE = 0
 MATH_CUDA = 1
 
+POLICY_GRIDWIDE_INDEPENDENT = 0
+POLICY_LEGACY_LOCAL = 1
+
 # CollapseState, reproducer.cpp:7455-7461 (216 bytes)
 STATS_FIELDS = ("internal_steps", "rhs_calls", "jacobian_calls", "decompositions",
                 "linear_solves", "accepted_steps", "rejected_steps")
@@ -91,8 +94,16 @@ def lib() -> ctypes.CDLL:
         L.wr_run_cells.argtypes = [vp, ctypes.c_int, ctypes.c_int, ip]
         L.wr_make_collapse_state.argtypes = [vp]
         L.wr_make_collapse_state.restype = None
+        L.wr_create_batch.argtypes = [ctypes.c_int, vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]
+        L.wr_grid_result.argtypes = [vp, ctypes.c_int, ip, ip]
+        L.wr_grid_dt_history.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int]
+        L.wr_make_batch_state.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_double, vp]
+        L.wr_make_batch_state.restype = None
         L.wr_set_profiling.argtypes = [vp, ctypes.c_int]
         L.wr_set_advance_variant.argtypes = [vp, ctypes.c_int]
+        L.wr_set_policy.argtypes = [vp, ctypes.c_int]
+        L.wr_autotune.argtypes = [vp, ctypes.c_int, ctypes.c_int, ip]
         L.wr_get_run_timing.argtypes = [vp, ctypes.POINTER(RunTiming)]
         L.wr_dt_history.argtypes = [vp, vp, ctypes.c_int]
         L.wr_diag_fp64_peak.argtypes = [dp]
@@ -125,15 +136,25 @@ def make_grid(grid_dim: int) -> np.ndarray:
 
 
 class Context:
-    """Device state for ``num_cells`` cells on one GPU (``wr_create`` .. ``wr_destroy``)."""
+    """Device state on one GPU (``wr_create`` .. ``wr_destroy``).
 
-    def __init__(self, num_cells: int, device: int = 0, math: int = MATH_PORTABLE):
+    ``Context(n)`` holds one grid of n cells.  ``Context(grids=[n0, n1, ...])``
+    batches several independent grids (``wr_create_batch``): cells are
+    concatenated grid after grid, each grid runs its own schedule, and one launch
+    covers all of them.
+    """
+
+    def __init__(self, num_cells: int = 0, device: int = 0, math: int = MATH_PORTABLE, grids=None):
         h = ctypes.c_void_p()
-        rc = lib().wr_create(int(num_cells), int(device), int(math), ctypes.byref(h))
+        if grids is None:
+            grids = [int(num_cells)]
+        sizes = np.ascontiguousarray(np.asarray(grids, dtype=np.int32))
+        rc = lib().wr_create_batch(len(sizes), sizes.ctypes.data, int(device), int(math), ctypes.byref(h))
         if rc != SUCCESS:
             raise WarpReactorError(rc, f"wr_create ({last_error()})")
         self.handle = h
-        self.num_cells = int(num_cells)
+        self.grids = [int(v) for v in sizes]
+        self.num_cells = int(sizes.sum())
 
     def close(self):
         if self.handle:
@@ -187,6 +208,20 @@ class Context:
         if rc != SUCCESS:
             raise WarpReactorError(rc, f"wr_set_advance_variant ({last_error()})")
 
+    def set_policy(self, policy: int) -> None:
+        """POLICY_GRIDWIDE_INDEPENDENT (default) or POLICY_LEGACY_LOCAL."""
+        rc = lib().wr_set_policy(self.handle, int(policy))
+        if rc != SUCCESS:
+            raise WarpReactorError(rc, f"wr_set_policy ({last_error()})")
+
+    def autotune(self, perturb: bool = True, steps: int = 24) -> int:
+        """Pick the fastest exact launch shape on the uploaded state; returns it."""
+        best = ctypes.c_int(-1)
+        rc = lib().wr_autotune(self.handle, int(bool(perturb)), int(steps), ctypes.byref(best))
+        if rc != SUCCESS:
+            raise WarpReactorError(rc, f"wr_autotune ({last_error()})")
+        return best.value
+
     def set_profiling(self, on: bool = True) -> None:
         rc = lib().wr_set_profiling(self.handle, int(bool(on)))
         if rc != SUCCESS:
@@ -197,12 +232,20 @@ class Context:
         lib().wr_get_run_timing(self.handle, ctypes.byref(t))
         return t
 
-    def dt_history(self) -> np.ndarray:
+    def dt_history(self, grid: int = 0) -> np.ndarray:
         out = np.zeros(MAX_COLLAPSE_STEPS)
-        rc = lib().wr_dt_history(self.handle, out.ctypes.data, MAX_COLLAPSE_STEPS)
+        rc = lib().wr_grid_dt_history(self.handle, int(grid), out.ctypes.data, MAX_COLLAPSE_STEPS)
         if rc != SUCCESS:
-            raise WarpReactorError(rc, f"wr_dt_history ({last_error()})")
+            raise WarpReactorError(rc, f"wr_grid_dt_history ({last_error()})")
         return out
+
+    def grid_result(self, grid: int):
+        """(IntegratorResult, completed_global_steps) of one grid after run()."""
+        cgs, res = ctypes.c_int(), ctypes.c_int()
+        rc = lib().wr_grid_result(self.handle, int(grid), ctypes.byref(cgs), ctypes.byref(res))
+        if rc != SUCCESS:
+            raise WarpReactorError(rc, f"wr_grid_result ({last_error()})")
+        return res.value, cgs.value
 
     def run(self, perturb: bool = True, completed_global_steps: int = 0):
         """The whole outer loop on the device -> (result, completed_global_steps)."""
@@ -219,6 +262,17 @@ def run_cells(cells: np.ndarray, perturb: bool = True, math: int = MATH_PORTABLE
         rc, cgs = ctx.run(perturb)
         ctx.download(cells)
     return rc, cgs
+
+
+def make_batch_grid(grid_id: int, num_cells: int, sigma_dex: float = 1.0, log10_tmin: float = 1.5,
+                    log10_tmax: float = 4.0) -> np.ndarray:
+    """Seeded cells of the batching workload (``wr_make_batch_state``): log-normal
+    density (sigma in dex) and log-uniform temperature."""
+    out = np.zeros(int(num_cells), COLLAPSE_STATE)
+    L = lib()
+    for i in range(int(num_cells)):
+        L.wr_make_batch_state(int(grid_id), i, sigma_dex, log10_tmin, log10_tmax, out[i:i + 1].ctypes.data)
+    return out
 
 
 def fp64_peak() -> float:

@@ -11,6 +11,13 @@
 //   --no-compare-final-state      (default for the GPU backend)
 //   --math portable|cuda          exp/log arithmetic (this program only;
 //                                 default portable, see warp_reactor.h)
+//   --driver-policy gridwide-independent|legacy-local
+//                                 outer-step policy (default gridwide-independent;
+//                                 legacy-local is the reference CPU program's)
+//   --write-final-state FILE      also write the packed final states to FILE with
+//                                 a FILE.manifest sidecar; refuses to overwrite
+//                                 either (the reference's Mojo program's flag,
+//                                 reproducer.mojo:3283-3330)
 //   -h | --help
 //
 // Output files: final_states_grid<N>_cuda.bin (grid > 1), rotated to
@@ -59,6 +66,8 @@ struct Options {
     bool perturb = true;
     bool show_help = false;
     int math = WR_MATH_PORTABLE;
+    int policy = WR_POLICY_GRIDWIDE_INDEPENDENT;
+    std::string write_path;
     std::string compare_path;  // the GPU backend compares only on request (:7467-7468)
 };
 
@@ -155,7 +164,9 @@ void print_stats(const std::vector<wr_collapse_state>& cells) {
 void print_usage(const char* program) {
     std::cerr << "usage: " << program
               << " [--grid N] [--perturb|--no-perturb]"
-                 " [--compare-final-state FILE|--no-compare-final-state]\n";
+                 " [--compare-final-state FILE|--no-compare-final-state]"
+                 " [--driver-policy gridwide-independent|legacy-local]"
+                 " [--write-final-state FILE] [--math portable|cuda]\n";
 }
 
 bool parse_positive_int(const char* text, int& value) {  // :8201-8211
@@ -216,6 +227,30 @@ bool parse_args(int argc, char** argv, Options& o) {  // :8229-8277
                 print_usage(argv[0]);
                 return false;
             }
+            continue;
+        }
+        if (arg == "--driver-policy") {
+            if (i + 1 >= argc) {
+                print_usage(argv[0]);
+                return false;
+            }
+            const std::string_view p{argv[++i]};
+            if (p == "gridwide-independent") {
+                o.policy = WR_POLICY_GRIDWIDE_INDEPENDENT;
+            } else if (p == "legacy-local") {
+                o.policy = WR_POLICY_LEGACY_LOCAL;
+            } else {
+                print_usage(argv[0]);
+                return false;
+            }
+            continue;
+        }
+        if (arg == "--write-final-state") {
+            if (i + 1 >= argc || argv[i + 1][0] == '\0') {
+                print_usage(argv[0]);
+                return false;
+            }
+            o.write_path = argv[++i];
             continue;
         }
         constexpr std::string_view prefix = "--compare-final-state=";
@@ -449,6 +484,49 @@ bool compare_from_file(const std::vector<wr_collapse_state>& cells, int grid, co
     return pass;
 }
 
+// Manifest sidecar of --write-final-state: what produced the records, so a
+// comparison can refuse files from a different program or policy (the Mojo
+// reference writes format, cell count, policy and source hashes,
+// reproducer.mojo:3283-3308).
+std::string manifest_contents(int num_cells, const Options& o) {
+    std::ostringstream m;
+    m << "format=packed-final-state-v1\n"
+      << "cell_count=" << num_cells << "\n"
+      << "policy=" << (o.policy == WR_POLICY_LEGACY_LOCAL ? "legacy-local" : "gridwide-independent") << "-v1\n"
+      << "perturbations=" << (o.perturb ? "enabled" : "disabled") << "\n"
+      << "math=" << (o.math == WR_MATH_CUDA ? "cuda" : "portable") << "\n"
+      << "program=reproducer_gb300\n";
+    return m.str();
+}
+
+bool write_with_manifest(const std::vector<wr_collapse_state>& cells, int grid, const std::string& path,
+                         const Options& o) {
+    namespace fs = std::filesystem;
+    std::error_code ec;
+    const std::string sidecar = path + ".manifest";
+    if (fs::exists(path, ec) || fs::exists(sidecar, ec)) {
+        std::cerr << "refusing to overwrite final-state output: " << path << "\n";
+        return false;
+    }
+    std::ofstream out(path, std::ios::binary);
+    if (!out) {
+        std::cerr << "failed to open final-state output file: " << path << "\n";
+        return false;
+    }
+    for (size_t c = 0; c < cells.size(); ++c) {
+        const wr_packed_final_state p = make_packed(cells[c], static_cast<int>(c), grid);
+        out.write(reinterpret_cast<const char*>(&p), sizeof p);
+    }
+    out.close();
+    std::ofstream man(sidecar);
+    man << manifest_contents(static_cast<int>(cells.size()), o);
+    if (!out || !man) {
+        std::cerr << "failed to write final-state output: " << path << "\n";
+        return false;
+    }
+    return true;
+}
+
 void print_state(const wr_collapse_state& s) {  // :8279-8287
     std::cout << "rho: " << s.rho << "\n";
     std::cout << "T: " << s.T << "\n";
@@ -489,6 +567,7 @@ int main(int argc, char** argv) {  // reproducer.cpp:8591-8702
         wr_ctx* ctx = nullptr;
         int device = 0;
         result = wr_create(num_cells, device, o.math, &ctx);
+        if (result == WR_SUCCESS) result = wr_set_policy(ctx, o.policy);
         if (result == WR_SUCCESS) result = wr_upload(ctx, cells.data());
         if (result == WR_SUCCESS) result = wr_run(ctx, o.perturb ? 1 : 0, &cgs);
         if (ctx) {
@@ -510,7 +589,8 @@ int main(int argc, char** argv) {  // reproducer.cpp:8591-8702
     std::cout << "Primordial chemistry collapse grid with ROS2S\n";
     std::cout << "grid: " << o.grid_dim << "^3 (" << num_cells << " cells)\n";
     std::cout << "perturbations: " << (o.perturb ? "enabled" : "disabled") << "\n";
-    std::cout << "driver policy: gridwide-independent\n";
+    std::cout << "driver policy: "
+              << (o.policy == WR_POLICY_LEGACY_LOCAL ? "legacy-local" : "gridwide-independent") << "\n";
     std::cout << "completed global collapse steps: " << cgs << "\n";
     print_collapse_summary(cells);
     std::cout << "wall time: " << elapsed << " s\n";
@@ -520,6 +600,10 @@ int main(int argc, char** argv) {  // reproducer.cpp:8591-8702
     if (!o.compare_path.empty()) {
         done = true;
         pass = compare_from_file(cells, o.grid_dim, o.compare_path);
+    }
+    if (!o.write_path.empty()) {
+        if (!write_with_manifest(cells, o.grid_dim, o.write_path, o)) return finish(false, done);
+        std::cout << "final states written: " << o.write_path << " (+ .manifest)\n";
     }
     if (o.grid_dim > 1) {
         std::ostringstream name;

@@ -4,8 +4,12 @@
 namespace wr {
 
 cudaError_t configure_advance_portable() {
-    return cudaFuncSetAttribute(k_advance<PortableMathCall, 128, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                static_cast<int>(advance_smem_bytes(0)));
+    cudaError_t e = cudaFuncSetAttribute(k_advance<PortableMathCall, 128, 1, true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(advance_smem_bytes(0)));
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_advance<PortableMathCall, 256, 1, true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                static_cast<int>(advance_smem_bytes(kPrecisionVariant)));
 }
 
 cudaError_t launch_advance_portable(int variant, int blocks, cudaStream_t stream, DevState s, StepCtl* ctl,
@@ -16,6 +20,10 @@ cudaError_t launch_advance_portable(int variant, int blocks, cudaStream_t stream
             break;
         case 2:
             k_advance<PortableMathCall, 256, 1, false><<<blocks, 256, 0, stream>>>(s, ctl, jbackup, ebuf);
+            break;
+        case 3:
+            k_advance<PortableMathCall, 256, 1, true, 1>
+                <<<blocks, 256, advance_smem_bytes(kPrecisionVariant), stream>>>(s, ctl, jbackup, ebuf);
             break;
         default:
             k_advance<PortableMathCall, 128, 1, true><<<blocks, 128, advance_smem_bytes(0), stream>>>(s, ctl, jbackup, ebuf);

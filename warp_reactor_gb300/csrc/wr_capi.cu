@@ -10,10 +10,12 @@
 
 #include <atomic>
 #include <cfloat>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "../../include/warp_reactor.h"
 #include "wr_launch.h"
@@ -41,6 +43,9 @@ constexpr int kCheckEvery = 16;
 
 struct wr_ctx {
     int n = 0;
+    int G = 1;                    // sub-grids batched in this context
+    int* grid_of = nullptr;       // device: sub-grid of each cell (G > 1)
+    int* grid_start = nullptr;    // device: first cell of each sub-grid (G > 1)
     int device = 0;
     int math = WR_MATH_PORTABLE;
     int advance_blocks = 0;
@@ -57,6 +62,13 @@ struct wr_ctx {
     wr_collapse_state* staging = nullptr;  // device AoS records for upload/download
     // optional per-kernel timing of wr_run (CUDA events on the context stream)
     bool profiling = false;
+    // CUDA graph of kCheckEvery outer steps (prepare, decide, order, advance,
+    // finalize per step), captured once per advance variant and replayed by wr_run
+    cudaGraphExec_t graph = nullptr;
+    int graph_variant = -1;
+    int graph_policy = -1;
+    int policy = WR_POLICY_GRIDWIDE_INDEPENDENT;
+    double* local_dt = nullptr;  // legacy-local policy: each cell's own dt
     cudaEvent_t ev[4 * WR_MAX_COLLAPSE_STEPS + 2] = {};
     int ev_used = 0;
     wr_run_timing timing{};
@@ -108,17 +120,17 @@ __global__ void k_pack(DevState s, wr_collapse_state* __restrict__ out) {
     out[i] = c;
 }
 
-// scatter the queued cells (those whose completed steps equal the grid's) into
-// the bucket order
+// scatter the cells k_prepare queued into the heaviest-first bucket order
 __global__ void k_order(DevState s, StepCtl* ctl) {
     const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= s.n || ctl->stop) return;
-    if (s.steps[cell] != ctl->cgs) return;
-    const unsigned int pos = atomicAdd(&ctl->off[cost_bucket(s.cost[cell])], 1u);
+    if (cell >= s.n || ctl->all_stop) return;
+    const int b = s.qbucket[cell];
+    if (b < 0) return;
+    const unsigned int pos = atomicAdd(&ctl->off[b], 1u);
     if (pos < static_cast<unsigned int>(s.n)) s.order[pos] = cell;
 }
 
-// start of an outer step driven by the host (wr_prepare)
+// start of an outer step driven by the host (wr_prepare; one grid)
 __global__ void k_begin_step(StepCtl* ctl, int cgs, double grid_time, int step, int perturb) {
     for (int b = 0; b < kBuckets; ++b) ctl->hist[b] = 0;
     ctl->cgs = cgs;
@@ -127,55 +139,96 @@ __global__ void k_begin_step(StepCtl* ctl, int cgs, double grid_time, int step, 
     ctl->perturb = perturb;
     ctl->dmin_bits = kDblMaxBits;
     ctl->stop = 0;
+    ctl->all_stop = 0;
 }
 
-// advance arguments driven by the host (wr_advance)
+// start of a device-driven run: every sub-grid at step 0
+__global__ void k_begin_run(StepCtl* ctl, int G, int cgs, int perturb) {
+    const int g = threadIdx.x;
+    if (g < G) {
+        StepCtl* c = ctl + g;
+        c->cgs = cgs;
+        c->grid_time = 0.0;
+        c->step = 0;
+        c->perturb = perturb;
+        c->dmin_bits = kDblMaxBits;
+        c->stop = 0;
+        c->integrated = 0;
+    }
+    if (g == 0) {
+        for (int b = 0; b < kBuckets; ++b) ctl->hist[b] = 0;
+        ctl->all_stop = 0;
+    }
+}
+
+// advance arguments driven by the host (wr_advance; one grid)
 __global__ void k_begin_advance(StepCtl* ctl, int cgs, double next_grid_time, double dt_grid) {
     ctl->cgs = cgs;
     ctl->next_grid_time = next_grid_time;
     ctl->dt_grid = dt_grid;
     ctl->integrated = 0;
     ctl->stop = 0;
+    ctl->all_stop = 0;
     build_queue_offsets(ctl);
 }
 
-// host checks between prepare and advance, reproducer.cpp:7880-7909
-__global__ void k_decide(StepCtl* ctl, double* dt_hist) {
-    if (ctl->stop) return;
-    if (ctl->failure != WR_SUCCESS) {
-        ctl->stop = 1;
+// host checks between prepare and advance, reproducer.cpp:7880-7909, one thread
+// per sub-grid
+__global__ void k_decide(StepCtl* ctl, int G, double* dt_hist, int legacy) {
+    const int g = threadIdx.x;
+    if (g == 0) build_queue_offsets(ctl);
+    if (g >= G) return;
+    StepCtl* c = ctl + g;
+    if (c->stop) return;
+    if (c->failure != WR_SUCCESS) {
+        c->stop = 1;
         return;
     }
-    if (ctl->dmin_bits == kDblMaxBits) {  // no candidate: the loop ends successfully
-        ctl->stop = 1;
+    if (legacy) {  // every cell has its own dt: no grid minimum
+        c->integrated = 0;
         return;
     }
-    const double dt = __longlong_as_double(static_cast<long long>(ctl->dmin_bits));
-    const double next = ctl->grid_time + dt;
+    if (c->dmin_bits == kDblMaxBits) {  // no candidate: the loop ends successfully
+        c->stop = 1;
+        return;
+    }
+    const double dt = __longlong_as_double(static_cast<long long>(c->dmin_bits));
+    const double next = c->grid_time + dt;
     if (!valid_positive(dt) || !isfinite(next)) {
-        ctl->failure = WR_BAD_INPUTS;
-        ctl->stop = 1;
+        c->failure = WR_BAD_INPUTS;
+        c->stop = 1;
         return;
     }
-    ctl->dt_grid = dt;
-    ctl->next_grid_time = next;
-    ctl->integrated = 0;
-    build_queue_offsets(ctl);
-    if (ctl->step >= 0 && ctl->step < WR_MAX_COLLAPSE_STEPS) dt_hist[ctl->step] = dt;
+    c->dt_grid = dt;
+    c->next_grid_time = next;
+    c->integrated = 0;
+    if (c->step >= 0 && c->step < WR_MAX_COLLAPSE_STEPS) dt_hist[g * WR_MAX_COLLAPSE_STEPS + c->step] = dt;
 }
 
-// host bookkeeping after the advance, reproducer.cpp:7930-7958
-__global__ void k_finalize(StepCtl* ctl, int max_steps) {
-    if (ctl->stop) return;
-    if (ctl->failure != WR_SUCCESS || ctl->integrated == 0) {
-        ctl->stop = 1;
-        return;
+// host bookkeeping after the advance, reproducer.cpp:7930-7958, one thread per
+// sub-grid; the run ends when every sub-grid has stopped
+__global__ void k_finalize(StepCtl* ctl, int G, int max_steps) {
+    __shared__ int running;
+    const int g = threadIdx.x;
+    if (g == 0) running = 0;
+    __syncthreads();
+    if (g < G) {
+        StepCtl* c = ctl + g;
+        if (!c->stop) {
+            if (c->failure != WR_SUCCESS || c->integrated == 0) {
+                c->stop = 1;
+            } else {
+                c->grid_time = c->next_grid_time;
+                c->cgs += 1;
+                c->step += 1;
+                c->dmin_bits = kDblMaxBits;
+                if (c->step >= max_steps) c->stop = 1;
+            }
+        }
+        if (!c->stop) atomicAdd(&running, 1);
     }
-    ctl->grid_time = ctl->next_grid_time;
-    ctl->cgs += 1;
-    ctl->step += 1;
-    ctl->dmin_bits = kDblMaxBits;
-    if (ctl->step >= max_steps) ctl->stop = 1;
+    __syncthreads();
+    if (g == 0) ctl->all_stop = running == 0;
 }
 
 }  // namespace wr
@@ -208,12 +261,29 @@ cudaError_t launch_order(wr_ctx* ctx) {
 cudaError_t launch_prepare(wr_ctx* ctx) {
     g_launches.fetch_add(1, std::memory_order_relaxed);
     const int blocks = (ctx->n + kPrepareThreads - 1) / kPrepareThreads;
-    k_prepare<kPrepareThreads><<<blocks > 0 ? blocks : 1, kPrepareThreads, 0, ctx->stream>>>(ctx->s, ctx->ctl);
+    if (ctx->policy == WR_POLICY_LEGACY_LOCAL)
+        k_prepare_legacy<kPrepareThreads><<<blocks > 0 ? blocks : 1, kPrepareThreads, 0, ctx->stream>>>(ctx->s, ctx->ctl);
+    else
+        k_prepare<kPrepareThreads><<<blocks > 0 ? blocks : 1, kPrepareThreads, 0, ctx->stream>>>(ctx->s, ctx->ctl);
     return cudaGetLastError();
 }
 
+cudaError_t reset_ctl(wr_ctx* ctx) {
+    std::vector<StepCtl> init(static_cast<size_t>(ctx->G));
+    for (auto& c : init) {
+        std::memset(&c, 0, sizeof c);
+        c.dmin_bits = kDblMaxBits;
+        c.failure = WR_SUCCESS;
+    }
+    cudaError_t e = cudaMemcpyAsync(ctx->ctl, init.data(), init.size() * sizeof(StepCtl), cudaMemcpyHostToDevice,
+                                    ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    return e;
+}
+
 int read_ctl(wr_ctx* ctx) {
-    cudaError_t e = cudaMemcpyAsync(ctx->host_ctl, ctx->ctl, sizeof(StepCtl), cudaMemcpyDeviceToHost, ctx->stream);
+    cudaError_t e = cudaMemcpyAsync(ctx->host_ctl, ctx->ctl, sizeof(StepCtl) * ctx->G, cudaMemcpyDeviceToHost,
+                                    ctx->stream);
     if (e != cudaSuccess) return fail("cudaMemcpyAsync(step control)", e);
     e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return fail("cudaStreamSynchronize", e);
@@ -229,13 +299,25 @@ const char* wr_last_error(void) { return g_last_error.c_str(); }
 uint64_t wr_kernel_launch_count(void) { return g_launches.load(); }
 
 int wr_create(int num_cells, int device, int math_mode, wr_ctx** out) {
+    return wr_create_batch(1, &num_cells, device, math_mode, out);
+}
+
+int wr_create_batch(int num_grids, const int* cells_per_grid, int device, int math_mode, wr_ctx** out) {
     if (!out) return fail_msg("wr_create: null output pointer");
     *out = nullptr;
-    if (num_cells <= 0) return fail_msg("wr_create: num_cells must be positive");
+    if (num_grids < 1 || num_grids > 1024 || !cells_per_grid) return fail_msg("wr_create_batch: 1..1024 grids");
+    long long total = 0;
+    for (int g = 0; g < num_grids; ++g) {
+        if (cells_per_grid[g] <= 0) return fail_msg("wr_create: num_cells must be positive");
+        total += cells_per_grid[g];
+    }
+    if (total > 0x7fffffffLL) return fail_msg("wr_create_batch: more than INT_MAX cells");
+    const int num_cells = static_cast<int>(total);
     if (math_mode != WR_MATH_PORTABLE && math_mode != WR_MATH_CUDA) return fail_msg("wr_create: unknown math mode");
     wr_ctx* ctx = new (std::nothrow) wr_ctx;
     if (!ctx) return fail_msg("wr_create: out of host memory");
     ctx->n = num_cells;
+    ctx->G = num_grids;
     ctx->device = device;
     ctx->math = math_mode;
     int rc = set_device(ctx);
@@ -248,8 +330,26 @@ int wr_create(int num_cells, int device, int math_mode, wr_ctx** out) {
         delete ctx;
         return fail("cudaStreamCreate", e);
     }
+    if (num_grids > 1) {
+        std::vector<int> of(static_cast<size_t>(num_cells)), start(static_cast<size_t>(num_grids));
+        int c0 = 0;
+        for (int g = 0; g < num_grids; ++g) {
+            start[g] = c0;
+            for (int i = 0; i < cells_per_grid[g]; ++i) of[c0 + i] = g;
+            c0 += cells_per_grid[g];
+        }
+        e = cudaMalloc(&ctx->grid_of, of.size() * sizeof(int));
+        if (e == cudaSuccess) e = cudaMalloc(&ctx->grid_start, start.size() * sizeof(int));
+        if (e == cudaSuccess) e = cudaMemcpy(ctx->grid_of, of.data(), of.size() * sizeof(int), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(ctx->grid_start, start.data(), start.size() * sizeof(int), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            wr_destroy(ctx);
+            return fail("wr_create_batch grid map", e);
+        }
+    }
     const size_t n = static_cast<size_t>(num_cells);
-    const size_t bytes = n * sizeof(double) * (3 + NS + 2) + n * sizeof(uint64_t) * 7 + n * sizeof(int) * 3;
+    const size_t bytes = n * sizeof(double) * (3 + NS + 2) + n * sizeof(uint64_t) * 7 + n * sizeof(int) * 4;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     ctx->sms = sms > 0 ? sms : 1;
@@ -260,11 +360,11 @@ int wr_create(int num_cells, int device, int math_mode, wr_ctx** out) {
         nslots = slots > nslots ? slots : nslots;
     }
     e = cudaMalloc(&ctx->state_buf, bytes);
-    if (e == cudaSuccess) e = cudaMalloc(&ctx->ctl, sizeof(StepCtl));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->ctl, sizeof(StepCtl) * ctx->G);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->jbackup, nslots * NEQ * NEQ * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->ebuf, nslots * NEQ * NEQ * sizeof(double));
-    if (e == cudaSuccess) e = cudaMalloc(&ctx->dt_hist, WR_MAX_COLLAPSE_STEPS * sizeof(double));
-    if (e == cudaSuccess) e = cudaMallocHost(&ctx->host_ctl, sizeof(StepCtl));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->dt_hist, static_cast<size_t>(ctx->G) * WR_MAX_COLLAPSE_STEPS * sizeof(double));
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->host_ctl, sizeof(StepCtl) * ctx->G);
     if (e == cudaSuccess) e = ctx->math == WR_MATH_CUDA ? configure_advance_cuda() : configure_advance_portable();
     if (e != cudaSuccess) {
         wr_destroy(ctx);
@@ -287,11 +387,10 @@ int wr_create(int num_cells, int device, int math_mode, wr_ctx** out) {
     ctx->s.steps = reinterpret_cast<int*>(take(n * sizeof(int)));
     ctx->s.cost = reinterpret_cast<int*>(take(n * sizeof(int)));
     ctx->s.order = reinterpret_cast<int*>(take(n * sizeof(int)));
-    StepCtl init{};
-    init.dmin_bits = kDblMaxBits;
-    init.failure = WR_SUCCESS;
-    e = cudaMemcpyAsync(ctx->ctl, &init, sizeof init, cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    ctx->s.qbucket = reinterpret_cast<int*>(take(n * sizeof(int)));
+    ctx->s.grid_of = ctx->grid_of;
+    ctx->s.grid_start = ctx->grid_start;
+    e = reset_ctl(ctx);
     if (e != cudaSuccess) {
         wr_destroy(ctx);
         return fail("wr_create init", e);
@@ -305,10 +404,14 @@ void wr_destroy(wr_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->profiling) wr_set_profiling(ctx, 0);
+    if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
     cudaFree(ctx->state_buf);
     cudaFree(ctx->ctl);
+    cudaFree(ctx->grid_of);
+    cudaFree(ctx->grid_start);
     cudaFree(ctx->jbackup);
     cudaFree(ctx->ebuf);
+    cudaFree(ctx->local_dt);
     cudaFree(ctx->dt_hist);
     cudaFree(ctx->staging);
     cudaFreeHost(ctx->host_ctl);
@@ -334,11 +437,7 @@ int wr_upload(wr_ctx* ctx, const wr_collapse_state* cells) {
     k_unpack<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->staging, ctx->s);
     e = cudaMemsetAsync(ctx->s.cost, 0, static_cast<size_t>(ctx->n) * sizeof(int), ctx->stream);
     if (e != cudaSuccess) return fail("cudaMemsetAsync(cost)", e);
-    StepCtl init{};
-    init.dmin_bits = kDblMaxBits;
-    init.failure = WR_SUCCESS;
-    e = cudaMemcpyAsync(ctx->ctl, &init, sizeof init, cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    e = reset_ctl(ctx);
     return e == cudaSuccess ? WR_SUCCESS : fail("wr_upload", e);
 }
 
@@ -358,6 +457,8 @@ int wr_download(wr_ctx* ctx, wr_collapse_state* cells) {
 int wr_prepare(wr_ctx* ctx, int completed_global_steps, double grid_time, int step, int perturb,
                double* dt_grid_out) {
     if (!ctx || !dt_grid_out) return fail_msg("wr_prepare: null argument");
+    if (ctx->G != 1 || ctx->policy != WR_POLICY_GRIDWIDE_INDEPENDENT)
+        return fail_msg("wr_prepare: host-stepped calls need a one-grid gridwide context");
     int rc = set_device(ctx);
     if (rc != WR_SUCCESS) return rc;
     g_launches.fetch_add(1, std::memory_order_relaxed);
@@ -375,6 +476,7 @@ int wr_prepare(wr_ctx* ctx, int completed_global_steps, double grid_time, int st
 int wr_advance(wr_ctx* ctx, int completed_global_steps, double next_grid_time, double dt_grid,
                int* integrated_out) {
     if (!ctx || !integrated_out) return fail_msg("wr_advance: null argument");
+    if (ctx->G != 1) return fail_msg("wr_advance: host-stepped calls need a one-grid context");
     int rc = set_device(ctx);
     if (rc != WR_SUCCESS) return rc;
     g_launches.fetch_add(1, std::memory_order_relaxed);
@@ -388,23 +490,98 @@ int wr_advance(wr_ctx* ctx, int completed_global_steps, double next_grid_time, d
     return ctx->host_ctl->failure;
 }
 
+// one outer step's launches (graph capture and the profiled path share them)
+static cudaError_t launch_step(wr_ctx* ctx) {
+    cudaError_t e = launch_prepare(ctx);
+    if (e == cudaSuccess) {
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        k_decide<<<1, 1024, 0, ctx->stream>>>(ctx->ctl, ctx->G, ctx->dt_hist,
+                                              ctx->policy == WR_POLICY_LEGACY_LOCAL);
+        e = launch_order(ctx);
+    }
+    if (e == cudaSuccess) e = launch_advance(ctx);
+    if (e == cudaSuccess) {
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        k_finalize<<<1, 1024, 0, ctx->stream>>>(ctx->ctl, ctx->G, WR_MAX_COLLAPSE_STEPS);
+        e = cudaGetLastError();
+    }
+    return e;
+}
+
+static int ensure_graph(wr_ctx* ctx) {
+    if (ctx->graph && ctx->graph_variant == ctx->variant && ctx->graph_policy == ctx->policy) return WR_SUCCESS;
+    if (ctx->graph) {
+        cudaGraphExecDestroy(ctx->graph);
+        ctx->graph = nullptr;
+    }
+    const uint64_t before = g_launches.load();
+    cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return fail("cudaStreamBeginCapture", e);
+    for (int i = 0; i < kCheckEvery && e == cudaSuccess; ++i) e = launch_step(ctx);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &graph);
+    g_launches.store(before);  // capture launches nothing
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return fail("graph capture", e != cudaSuccess ? e : e2);
+    }
+    e = cudaGraphInstantiate(&ctx->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail("cudaGraphInstantiate", e);
+    ctx->graph_variant = ctx->variant;
+    ctx->graph_policy = ctx->policy;
+    return WR_SUCCESS;
+}
+
+// wr_run without per-kernel timing: chunks of kCheckEvery outer steps replayed
+// from a CUDA graph, one 64-byte-per-grid status read between chunks
+static int run_graph(wr_ctx* ctx, int perturb, int* completed_global_steps) {
+    int rc = ensure_graph(ctx);
+    if (rc != WR_SUCCESS) return rc;
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    k_begin_run<<<1, 1024, 0, ctx->stream>>>(ctx->ctl, ctx->G, *completed_global_steps, perturb ? 1 : 0);
+    for (int done = 0; done < WR_MAX_COLLAPSE_STEPS; done += kCheckEvery) {
+        cudaError_t e = cudaGraphLaunch(ctx->graph, ctx->stream);
+        if (e != cudaSuccess) return fail("cudaGraphLaunch", e);
+        g_launches.fetch_add(5 * kCheckEvery, std::memory_order_relaxed);
+        rc = read_ctl(ctx);
+        if (rc != WR_SUCCESS) return rc;
+        if (ctx->host_ctl->all_stop) break;
+    }
+    *completed_global_steps = ctx->host_ctl->cgs;
+    for (int g = 0; g < ctx->G; ++g)
+        if (ctx->host_ctl[g].failure != WR_SUCCESS) return ctx->host_ctl[g].failure;
+    return WR_SUCCESS;
+}
+
+static int run_profiled(wr_ctx* ctx, int perturb, int max_steps, int* completed_global_steps);
+
 int wr_run(wr_ctx* ctx, int perturb, int* completed_global_steps) {
     if (!ctx || !completed_global_steps) return fail_msg("wr_run: null argument");
     int rc = set_device(ctx);
     if (rc != WR_SUCCESS) return rc;
+    if (!ctx->profiling) return run_graph(ctx, perturb, completed_global_steps);
+    return run_profiled(ctx, perturb, WR_MAX_COLLAPSE_STEPS, completed_global_steps);
+}
+
+// launch by launch, with CUDA events around every kernel when profiling; stops
+// after max_steps outer steps (the autotuner's short runs)
+static int run_profiled(wr_ctx* ctx, int perturb, int max_steps, int* completed_global_steps) {
+    int rc = WR_SUCCESS;
     g_launches.fetch_add(1, std::memory_order_relaxed);
     const int nev = 4 * WR_MAX_COLLAPSE_STEPS + 2;
     ctx->ev_used = 0;
     record(ctx, nev - 2);
-    k_begin_step<<<1, 1, 0, ctx->stream>>>(ctx->ctl, *completed_global_steps, 0.0, 0, perturb ? 1 : 0);
+    k_begin_run<<<1, 1024, 0, ctx->stream>>>(ctx->ctl, ctx->G, *completed_global_steps, perturb ? 1 : 0);
     int steps_launched = 0;
-    for (int step = 0; step < WR_MAX_COLLAPSE_STEPS; ++step) {
+    for (int step = 0; step < max_steps; ++step) {
         record(ctx, 4 * step + 0);
         cudaError_t e = launch_prepare(ctx);
         record(ctx, 4 * step + 1);
         if (e == cudaSuccess) {
             g_launches.fetch_add(1, std::memory_order_relaxed);
-            k_decide<<<1, 1, 0, ctx->stream>>>(ctx->ctl, ctx->dt_hist);
+            k_decide<<<1, 1024, 0, ctx->stream>>>(ctx->ctl, ctx->G, ctx->dt_hist,
+                                                  ctx->policy == WR_POLICY_LEGACY_LOCAL);
             e = launch_order(ctx);
             record(ctx, 4 * step + 2);
             if (e == cudaSuccess) e = launch_advance(ctx);
@@ -413,14 +590,14 @@ int wr_run(wr_ctx* ctx, int perturb, int* completed_global_steps) {
         steps_launched = step + 1;
         if (e == cudaSuccess) {
             g_launches.fetch_add(1, std::memory_order_relaxed);
-            k_finalize<<<1, 1, 0, ctx->stream>>>(ctx->ctl, WR_MAX_COLLAPSE_STEPS);
+            k_finalize<<<1, 1024, 0, ctx->stream>>>(ctx->ctl, ctx->G, max_steps);
             e = cudaGetLastError();
         }
         if (e != cudaSuccess) return fail("step launch", e);
-        if ((step + 1) % kCheckEvery == 0 || step + 1 == WR_MAX_COLLAPSE_STEPS) {
+        if ((step + 1) % kCheckEvery == 0 || step + 1 == max_steps) {
             rc = read_ctl(ctx);
             if (rc != WR_SUCCESS) return rc;
-            if (ctx->host_ctl->stop) break;
+            if (ctx->host_ctl->all_stop) break;
         }
     }
     record(ctx, nev - 1);
@@ -443,7 +620,91 @@ int wr_run(wr_ctx* ctx, int perturb, int* completed_global_steps) {
         ctx->timing = t;
     }
     *completed_global_steps = ctx->host_ctl->cgs;
-    return ctx->host_ctl->failure;
+    for (int g = 0; g < ctx->G; ++g)
+        if (ctx->host_ctl[g].failure != WR_SUCCESS) return ctx->host_ctl[g].failure;
+    return WR_SUCCESS;
+}
+
+int wr_grid_result(wr_ctx* ctx, int grid, int* completed_global_steps, int* result) {
+    if (!ctx || !completed_global_steps || !result || grid < 0 || grid >= ctx->G)
+        return fail_msg("wr_grid_result: bad argument");
+    int rc = set_device(ctx);
+    if (rc == WR_SUCCESS) rc = read_ctl(ctx);
+    if (rc != WR_SUCCESS) return rc;
+    *completed_global_steps = ctx->host_ctl[grid].cgs;
+    *result = ctx->host_ctl[grid].failure;
+    return WR_SUCCESS;
+}
+
+int wr_grid_dt_history(wr_ctx* ctx, int grid, double* out, int max_steps) {
+    if (!ctx || !out || max_steps < 0 || grid < 0 || grid >= ctx->G) return fail_msg("wr_grid_dt_history: bad argument");
+    int rc = set_device(ctx);
+    if (rc != WR_SUCCESS) return rc;
+    const int n = max_steps < WR_MAX_COLLAPSE_STEPS ? max_steps : WR_MAX_COLLAPSE_STEPS;
+    cudaError_t e = cudaMemcpyAsync(out, ctx->dt_hist + static_cast<size_t>(grid) * WR_MAX_COLLAPSE_STEPS,
+                                    n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    return e == cudaSuccess ? WR_SUCCESS : fail("wr_grid_dt_history", e);
+}
+
+int wr_autotune(wr_ctx* ctx, int perturb, int steps, int* best_variant) {
+    if (!ctx || !best_variant || steps < 1) return fail_msg("wr_autotune: bad argument");
+    int rc = set_device(ctx);
+    if (rc != WR_SUCCESS) return rc;
+    const size_t bytes = static_cast<size_t>(ctx->n) * ((3 + NS + 2) * sizeof(double) + 7 * sizeof(uint64_t) + 4 * sizeof(int));
+    void* snap = nullptr;
+    cudaError_t e = cudaMalloc(&snap, bytes);
+    if (e != cudaSuccess) return fail("wr_autotune snapshot", e);
+    e = cudaMemcpyAsync(snap, ctx->state_buf, bytes, cudaMemcpyDeviceToDevice, ctx->stream);
+    const bool was_profiling = ctx->profiling;
+    const int keep = ctx->variant;
+    if (e == cudaSuccess && !was_profiling) rc = wr_set_profiling(ctx, 1);
+    double best_ms = 1e300;
+    int best = keep;
+    // candidates: the exact (FP64) launch shapes; the precision form is a
+    // different arithmetic and is chosen explicitly, never by the tuner
+    for (int v = 0; e == cudaSuccess && rc == WR_SUCCESS && v < kPrecisionVariant; ++v) {
+        e = cudaMemcpyAsync(ctx->state_buf, snap, bytes, cudaMemcpyDeviceToDevice, ctx->stream);
+        if (e != cudaSuccess) break;
+        rc = reset_ctl(ctx) == cudaSuccess ? WR_SUCCESS : WR_BAD_INPUTS;
+        if (rc != WR_SUCCESS) break;
+        ctx->variant = v;
+        int cgs = 0;
+        rc = run_profiled(ctx, perturb, steps, &cgs);
+        if (rc != WR_SUCCESS) break;
+        if (ctx->timing.advance_ms < best_ms) {
+            best_ms = ctx->timing.advance_ms;
+            best = v;
+        }
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->state_buf, snap, bytes, cudaMemcpyDeviceToDevice, ctx->stream);
+    if (e == cudaSuccess) e = reset_ctl(ctx);
+    cudaFree(snap);
+    if (!was_profiling) wr_set_profiling(ctx, 0);
+    if (e != cudaSuccess) return fail("wr_autotune", e);
+    if (rc != WR_SUCCESS) {
+        ctx->variant = keep;
+        return rc;
+    }
+    ctx->variant = best;
+    *best_variant = best;
+    return WR_SUCCESS;
+}
+
+int wr_set_policy(wr_ctx* ctx, int policy) {
+    if (!ctx) return fail_msg("wr_set_policy: null context");
+    if (policy != WR_POLICY_GRIDWIDE_INDEPENDENT && policy != WR_POLICY_LEGACY_LOCAL)
+        return fail_msg("wr_set_policy: unknown policy");
+    if (policy == WR_POLICY_LEGACY_LOCAL && ctx->G != 1) return fail_msg("wr_set_policy: legacy-local needs one grid");
+    int rc = set_device(ctx);
+    if (rc != WR_SUCCESS) return rc;
+    if (policy == WR_POLICY_LEGACY_LOCAL && !ctx->local_dt) {
+        const cudaError_t e = cudaMalloc(&ctx->local_dt, static_cast<size_t>(ctx->n) * sizeof(double));
+        if (e != cudaSuccess) return fail("cudaMalloc(local dt)", e);
+    }
+    ctx->policy = policy;
+    ctx->s.local_dt = policy == WR_POLICY_LEGACY_LOCAL ? ctx->local_dt : nullptr;
+    return WR_SUCCESS;
 }
 
 int wr_set_advance_variant(wr_ctx* ctx, int variant) {
@@ -541,6 +802,42 @@ void wr_make_collapse_state(wr_collapse_state* out) {
     out->time = 0.0;
     out->density_driver = rho;
     out->completed_steps = 0;
+}
+
+// Seeded initial cells of the batching workload: the reference's initial cell
+// (make_collapse_state) with its density scaled by a log-normal factor
+// 10^(sigma_dex * N(0,1)) and its temperature drawn log-uniformly in
+// [10^log10_tmin, 10^log10_tmax]; the energy follows from the EOS (eos_rt,
+// reproducer.cpp:306-309).  Streams: splitmix64 of (cell, grid_id), Box-Muller
+// for the normal deviate.  Host code; the same array feeds the GPU and the oracle.
+void wr_make_batch_state(int grid_id, int cell, double sigma_dex, double log10_tmin, double log10_tmax,
+                         wr_collapse_state* out) {
+    wr_make_collapse_state(out);
+    const uint64_t seed = (static_cast<uint64_t>(static_cast<unsigned int>(cell)) << 32U) ^
+                          (static_cast<uint64_t>(static_cast<unsigned int>(grid_id) + 1U) << 8U) ^
+                          0x5bd1e9955bd1e995ULL;
+    double u[3];
+    for (int k = 0; k < 3; ++k) {
+        const uint64_t bits = splitmix64(seed + 0x632be59bd9b4e019ULL * static_cast<uint64_t>(k + 1)) >> 11U;
+        u[k] = static_cast<double>(bits) * (1.0 / 9007199254740992.0);
+    }
+    const double two_pi = 6.283185307179586476925286766559;
+    const double normal = std::sqrt(-2.0 * std::log(1.0 - u[0])) * std::cos(two_pi * u[1]);
+    const double mult = std::pow(10.0, sigma_dex * normal);
+    for (int k = 0; k < NS; ++k) out->xn[k] *= mult;
+    out->rho *= mult;
+    out->density_driver = out->rho;
+    const double T = std::pow(10.0, log10_tmin + (log10_tmax - log10_tmin) * u[2]);
+    double sa = 0.0, sg = 0.0, rt = 0.0;
+    for (int k = 0; k < NS; ++k) rt += out->xn[k] * mass(k);
+    for (int k = 0; k < NS; ++k) {
+        sa += out->xn[k];
+        sg += (out->xn[k] * kMp / rt) * inv_gm1(k);
+    }
+    sa *= kMp / rt;
+    sg /= sa;
+    out->T = T;
+    out->e = sg * sa * kGasConstant * T;
 }
 
 }  // extern "C"

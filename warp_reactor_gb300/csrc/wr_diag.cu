@@ -92,6 +92,26 @@ __global__ void k_diag_div(int n, const double* __restrict__ a, const double* __
     if (i < n) out[i] = ddiv(a[i], b[i]);
 }
 
+// one block of `warps` warps, each lane running C independent dependent FMA chains;
+// clock64 cycles per iteration tell the per-warp FP64 issue interval
+template <int C>
+__global__ void k_fp64_issue(double* out, long long* cyc, int iters) {
+    double x[C];
+#pragma unroll
+    for (int c = 0; c < C; ++c) x[c] = threadIdx.x * 1e-3 + c;
+    const long long t0 = clock64();
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int c = 0; c < C; ++c) x[c] = fma(x[c], 0.999999, 1.0e-7);
+    }
+    const long long t1 = clock64();
+    double s = 0.0;
+#pragma unroll
+    for (int c = 0; c < C; ++c) s += x[c];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+    if (threadIdx.x == 0) cyc[blockIdx.x] = t1 - t0;
+}
+
 thread_local std::string g_diag_error;
 
 struct DevBuf {
@@ -210,6 +230,25 @@ int wr_diag_flush_l2(int mib) {
     cudaError_t e = cudaMemset(buf, mib & 0xff, bytes);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     return e == cudaSuccess ? WR_SUCCESS : diag_fail("wr_diag_flush_l2", e);
+}
+
+int wr_diag_fp64_issue(int warps, int chains, double* cycles_per_instr) {
+    if (warps < 1 || warps > 32 || !cycles_per_instr || (chains != 1 && chains != 4 && chains != 8)) return WR_BAD_INPUTS;
+    DevBuf out, cyc;
+    cudaError_t e = cudaMalloc(&out.p, static_cast<size_t>(warps) * 32 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&cyc.p, sizeof(long long));
+    if (e != cudaSuccess) return diag_fail("wr_diag_fp64_issue", e);
+    const int iters = 2048;
+    for (int rep = 0; rep < 2; ++rep) {  // the first launch warms up
+        if (chains == 1) k_fp64_issue<1><<<1, warps * 32>>>((double*)out.p, (long long*)cyc.p, iters);
+        else if (chains == 4) k_fp64_issue<4><<<1, warps * 32>>>((double*)out.p, (long long*)cyc.p, iters);
+        else k_fp64_issue<8><<<1, warps * 32>>>((double*)out.p, (long long*)cyc.p, iters);
+    }
+    long long c = 0;
+    e = cudaMemcpy(&c, cyc.p, sizeof c, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return diag_fail("wr_diag_fp64_issue", e);
+    *cycles_per_instr = static_cast<double>(c) / (static_cast<double>(iters) * chains);
+    return WR_SUCCESS;
 }
 
 int wr_diag_fp64_peak(double* dfma_per_s) {

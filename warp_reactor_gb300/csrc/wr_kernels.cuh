@@ -49,7 +49,14 @@ struct DevState {
     uint64_t* stats;  // [7][n]
     int* cost;        // ROS2S attempts of the cell's last burn (scheduling hint)
     int* order;       // advance work queue: cells of this step, heaviest first
+    int* qbucket;     // queue bucket chosen by k_prepare for this step (-1: not queued)
+    const int* grid_of;    // sub-grid of each cell (nullptr: one grid)
+    const int* grid_start; // first cell of each sub-grid (nullptr: one grid)
+    double* local_dt;      // legacy-local policy: each cell's own dt (nullptr: gridwide)
     int n;
+    // index of the cell within its own sub-grid is cell - grid_base(g): the
+    // perturbation seed of the reference uses the cell's index in its grid
+    __device__ __forceinline__ int grid_base(int g) const { return grid_start ? grid_start[g] : 0; }
 };
 
 // Work-queue order: cells are bucketed by last step's attempt count, heaviest
@@ -71,10 +78,12 @@ struct StepCtl {
     double grid_time;
     double dt_grid;
     double next_grid_time;
-    unsigned int queue;            // work-queue head of k_advance
-    unsigned int queued;           // cells in the work queue of this step
-    unsigned int hist[kBuckets];   // queued cells per cost bucket (k_prepare)
-    unsigned int off[kBuckets];    // bucket start offsets in `order`
+    unsigned int queue;            // work-queue head of k_advance (ctl[0] only)
+    unsigned int queued;           // cells in the work queue of this step (ctl[0] only)
+    int all_stop;                  // every sub-grid has stopped (ctl[0] only)
+    int pad_;
+    unsigned int hist[kBuckets];   // queued cells per cost bucket (k_prepare; ctl[0] only)
+    unsigned int off[kBuckets];    // bucket start offsets in `order` (ctl[0] only)
 };
 
 constexpr unsigned long long kDblMaxBits = 0x7fefffffffffffffULL;
@@ -118,34 +127,37 @@ __device__ __forceinline__ void record_failure(StepCtl* ctl, int code) {
     atomicCAS(&ctl->failure, WR_SUCCESS, code);
 }
 
+// One prepare pass over all cells.  With several sub-grids batched in one state
+// (s.grid_of != nullptr), each cell reads and reduces into its own sub-grid's
+// control block; a warp whose lanes all belong to one sub-grid reduces with
+// shuffles and issues one atomic, other warps (sub-grid boundaries) issue one
+// atomic per lane.  The queue histogram is global (ctl[0]).
 template <int B>
 __global__ void __launch_bounds__(B) k_prepare(DevState s, StepCtl* ctl) {
-    __shared__ unsigned long long red[B / 32];
     __shared__ unsigned int hist[kBuckets];
     for (int i = threadIdx.x; i < kBuckets; i += B) hist[i] = 0;
     __syncthreads();
-    const int stop = ctl->stop;
-    const int cgs = ctl->cgs;
-    const double grid_time = ctl->grid_time;
-    const int step = ctl->step;
-    const bool perturb = ctl->perturb != 0;
-    const int failure0 = ctl->failure;
     const int cell = blockIdx.x * B + threadIdx.x;
+    const int g = (s.grid_of != nullptr && cell < s.n) ? s.grid_of[cell] : 0;
+    StepCtl* c = ctl + g;
     unsigned long long cand = kDblMaxBits;
-    if (!stop && failure0 == WR_SUCCESS && cell < s.n) {
+    int bucket = -1;
+    if (cell < s.n && !c->stop && c->failure == WR_SUCCESS) {
         const int n = s.n;
+        const int cgs = c->cgs;
+        const int step = c->step;
         const int cs = s.steps[cell];
         if (cs >= cgs) {
-            if (cs != cgs || s.time[cell] != grid_time) {
-                record_failure(ctl, WR_BAD_INPUTS);
+            if (cs != cgs || s.time[cell] != c->grid_time) {
+                record_failure(c, WR_BAD_INPUTS);
             } else {
                 double xn[NS];
 #pragma unroll
                 for (int k = 0; k < NS; ++k) xn[k] = s.xn[k * n + cell];
                 double driver = s.driver[cell];
                 // apply_perturbation, reproducer.cpp:7564-7580
-                if (perturb && step != 0 && step % kPerturbInterval == 0) {
-                    const double factor = perturbation_factor(cell, step);
+                if (c->perturb && step != 0 && step % kPerturbInterval == 0) {
+                    const double factor = perturbation_factor(cell - s.grid_base(g), step);
                     driver *= factor;
                     const double rho = s.rho[cell] * factor;
 #pragma unroll
@@ -159,7 +171,7 @@ __global__ void __launch_bounds__(B) k_prepare(DevState s, StepCtl* ctl) {
                 }
                 const double dt = collapse_timestep(xn);
                 if (!valid_positive(dt) || !valid_positive(driver)) {
-                    record_failure(ctl, WR_BAD_INPUTS);
+                    record_failure(c, WR_BAD_INPUTS);
                 } else if (dt < 10.0) {
                     const double tff = ddiv(dt, kTffReduc);
                     driver += dt * ddiv(driver, tff);
@@ -167,24 +179,83 @@ __global__ void __launch_bounds__(B) k_prepare(DevState s, StepCtl* ctl) {
                     cand = static_cast<unsigned long long>(__double_as_longlong(dt));
                 }
                 s.driver[cell] = driver;
-                atomicAdd(&hist[cost_bucket(s.cost[cell])], 1u);
+                bucket = cost_bucket(s.cost[cell]);
+                atomicAdd(&hist[bucket], 1u);
             }
         }
     }
-    // block minimum of positive-double bit patterns, then one atomic per block
+    if (cell < s.n) s.qbucket[cell] = bucket;
+    // minimum of positive-double bit patterns per sub-grid
+    const int g0 = __shfl_sync(0xffffffffu, g, 0);
+    if (__all_sync(0xffffffffu, g == g0)) {
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        const unsigned long long o = __shfl_xor_sync(0xffffffffu, cand, off);
-        cand = o < cand ? o : cand;
+        for (int off = 16; off > 0; off >>= 1) {
+            const unsigned long long o = __shfl_xor_sync(0xffffffffu, cand, off);
+            cand = o < cand ? o : cand;
+        }
+        if ((threadIdx.x & 31) == 0 && cand != kDblMaxBits) atomicMin(&c->dmin_bits, cand);
+    } else if (cand != kDblMaxBits) {
+        atomicMin(&c->dmin_bits, cand);
     }
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = cand;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned long long m = red[0];
+    for (int i = threadIdx.x; i < kBuckets; i += B)
+        if (hist[i]) atomicAdd(&ctl->hist[i], hist[i]);
+}
+
+// Prepare of the legacy-local policy (the reference CPU program's default,
+// advance_collapse_step up to the burn, reproducer.cpp:7646-7670): each cell
+// perturbs, takes its own free-fall dt and density update, and either stops
+// (dt < 10 s or density limit) or is queued with its scaled state and dt.
+template <int B>
+__global__ void __launch_bounds__(B) k_prepare_legacy(DevState s, StepCtl* ctl) {
+    __shared__ unsigned int hist[kBuckets];
+    for (int i = threadIdx.x; i < kBuckets; i += B) hist[i] = 0;
+    __syncthreads();
+    const int cell = blockIdx.x * B + threadIdx.x;
+    int bucket = -1;
+    if (cell < s.n && !ctl->stop && ctl->failure == WR_SUCCESS && s.steps[cell] >= ctl->cgs) {
+        const int n = s.n;
+        const int step = ctl->step;
+        double xn[NS];
 #pragma unroll
-        for (int w = 1; w < B / 32; ++w) m = red[w] < m ? red[w] : m;
-        if (m != kDblMaxBits) atomicMin(&ctl->dmin_bits, m);
+        for (int k = 0; k < NS; ++k) xn[k] = s.xn[k * n + cell];
+        double driver = s.driver[cell];
+        double rho = s.rho[cell];
+        bool changed = false;
+        if (ctl->perturb && step != 0 && step % kPerturbInterval == 0) {
+            const double factor = perturbation_factor(cell, step);
+            driver *= factor;
+            rho = rho * factor;
+#pragma unroll
+            for (int k = 0; k < NS; ++k) xn[k] *= factor;
+            renormalize(xn, rho);
+            s.T[cell] = eos_T_from_e(xn, s.e[cell]);
+            changed = true;
+        }
+        const double old_density = driver;
+        const double dt = collapse_timestep(xn);
+        const double tff = ddiv(dt, kTffReduc);
+        driver += dt * ddiv(driver, tff);
+        if (!(dt < 10.0 || driver > kDriverLimit)) {
+            const double ratio = ddiv(driver, old_density);
+#pragma unroll
+            for (int k = 0; k < NS; ++k) xn[k] *= ratio;
+            rho *= ratio;
+            s.e[cell] = eos_e_from_T(xn, s.T[cell]);  // burn_ros2s prologue (eos_rt)
+            s.local_dt[cell] = dt;
+            changed = true;
+            bucket = cost_bucket(s.cost[cell]);
+            atomicAdd(&hist[bucket], 1u);
+        }
+        s.driver[cell] = driver;
+        if (changed) {
+            s.rho[cell] = rho;
+#pragma unroll
+            for (int k = 0; k < NS; ++k) s.xn[k * n + cell] = xn[k];
+        }
     }
+    if (cell < s.n) s.qbucket[cell] = bucket;
+    __syncthreads();
     for (int i = threadIdx.x; i < kBuckets; i += B)
         if (hist[i]) atomicAdd(&ctl->hist[i], hist[i]);
 }
@@ -233,6 +304,13 @@ struct JSink {
         E(r, c) = -v;
         jb[(r * NEQ + c) * stride] = v;
     }
+};
+
+// J sink of the precision form: J only into the lane's FP64 global backup
+struct JBackupSink {
+    double* jb;
+    int stride;
+    __device__ __forceinline__ void operator()(int r, int c, double v) { jb[(r * NEQ + c) * stride] = v; }
 };
 
 // burn_state_from_y (reproducer.cpp:7029-7038): floored X and T from y
@@ -322,6 +400,111 @@ __device__ __forceinline__ void lu_solve(MT LU, const uint64_t ip, double* x) {
     }
 }
 
+// ---------------------------------------------------------------- precision form
+// The iteration matrix factorised in FP32 (shared memory, 900 B per lane), with
+// one FP64 residual refinement per stage solve; J itself stays FP64 in the lane's
+// global backup, from which both the FP32 matrix and the FP64 residual are built.
+template <int B>
+struct MatF {
+    float* base;
+    __device__ __forceinline__ float& operator()(int r, int c) const { return base[(r * NEQ + c) * B]; }
+};
+
+template <class MT>
+__device__ __forceinline__ int lu_decompose_f32(MT A, uint64_t& ip) {
+    int info = 0;
+    uint64_t piv = 0;
+#pragma unroll 1
+    for (int k = 0; k < NEQ - 1; ++k) {
+        int p = k;
+        float maxv = fabsf(A(k, k));
+#pragma unroll 1
+        for (int i = k + 1; i < NEQ; ++i) {
+            const float v = fabsf(A(i, k));
+            if (v > maxv) {
+                maxv = v;
+                p = i;
+            }
+        }
+        piv |= static_cast<uint64_t>(p) << (4 * k);
+        if (A(p, k) != 0.0f) {
+            if (p != k) {
+#pragma unroll 1
+                for (int j = k; j < NEQ; ++j) {
+                    const float t = A(p, j);
+                    A(p, j) = A(k, j);
+                    A(k, j) = t;
+                }
+            }
+            const float mult = -1.0f / A(k, k);
+#pragma unroll 1
+            for (int i = k + 1; i < NEQ; ++i) A(i, k) = A(i, k) * mult;
+#pragma unroll 1
+            for (int j = k + 1; j < NEQ; ++j) {
+                const float t = A(k, j);
+#pragma unroll 4
+                for (int i = k + 1; i < NEQ; ++i) A(i, j) = fmaf(t, A(i, k), A(i, j));
+            }
+        } else {
+            info = k + 1;
+        }
+    }
+    piv |= static_cast<uint64_t>(NEQ - 1) << (4 * (NEQ - 1));
+    if (A(NEQ - 1, NEQ - 1) == 0.0f) info = NEQ;
+    ip = piv;
+    return info;
+}
+
+template <class MT>
+__device__ __forceinline__ void lu_solve_f32(MT LU, const uint64_t ip, float* x) {
+#pragma unroll
+    for (int k = 0; k < NEQ - 1; ++k) {
+        const int p = static_cast<int>((ip >> (4 * k)) & 15);
+        float t = x[k];
+#pragma unroll
+        for (int i = k + 1; i < NEQ; ++i) t = (p == i) ? x[i] : t;
+        if (p != k) {
+#pragma unroll
+            for (int i = k + 1; i < NEQ; ++i) x[i] = (p == i) ? x[k] : x[i];
+            x[k] = t;
+        }
+#pragma unroll
+        for (int j = k + 1; j < NEQ; ++j) x[j] = fmaf(t, LU(j, k), x[j]);
+    }
+#pragma unroll
+    for (int kb = 0; kb < NEQ; ++kb) {
+        const int k = NEQ - 1 - kb;
+        x[k] = x[k] / LU(k, k);
+        const float t = -x[k];
+#pragma unroll
+        for (int j = 0; j < k; ++j) x[j] = fmaf(t, LU(j, k), x[j]);
+    }
+}
+
+// x <- E^-1 x with E = fac*I - J: FP32 solve, FP64 residual b - E x0 (J from the
+// lane's FP64 backup), FP32 correction
+template <class MT>
+__device__ __forceinline__ void solve_refined(MT LU, const uint64_t ip, const double* jb, int stride, double fac,
+                                              double* x) {
+    float xf[NEQ];
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i) xf[i] = __double2float_rn(x[i]);
+    lu_solve_f32(LU, ip, xf);
+    double x0[NEQ];
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i) x0[i] = static_cast<double>(xf[i]);
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i) {
+        double acc = 0.0;
+#pragma unroll
+        for (int j = 0; j < NEQ; ++j) acc = acc + jb[(i * NEQ + j) * stride] * x0[j];
+        xf[i] = __double2float_rn(x[i] - (fac * x0[i] - acc));
+    }
+    lu_solve_f32(LU, ip, xf);
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i) x[i] = x0[i] + static_cast<double>(xf[i]);
+}
+
 struct Lane {
     // ROS2S controller state of RODAS::integrate (reproducer.cpp:7225-7235)
     double x, h, hacc, erracc, hopt, tout;
@@ -333,21 +516,21 @@ struct Lane {
 //   B threads per block, MINB resident blocks per SM (register budget), SMEM_E
 //   whether the per-lane iteration matrix lives in shared memory (225 doubles per
 //   lane) or in the global per-lane array `ebuf`.
-template <class M, int B, int MINB, bool SMEM_E>
+//   PREC 0: FP64 factorisation (the plain form); 1: FP32 factorisation in shared
+//   memory with one FP64 residual refinement per stage solve (the precision form).
+template <class M, int B, int MINB, bool SMEM_E, int PREC = 0>
 __global__ void __launch_bounds__(B, MINB) k_advance(DevState s, StepCtl* ctl, double* __restrict__ jbackup,
                                                    double* __restrict__ ebuf) {
     extern __shared__ double smem[];
-    using MT = typename std::conditional<SMEM_E, Mat<B>, MatG>::type;
-    if (ctl->stop) return;
+    using MT = typename std::conditional<SMEM_E && PREC == 0, Mat<B>, MatG>::type;
+    MatF<B> E32{reinterpret_cast<float*>(smem) + threadIdx.x};
+    if (ctl->all_stop) return;
     const int n = s.n;
-    const int cgs = ctl->cgs;
-    const double dt_grid = ctl->dt_grid;
-    const double next_grid_time = ctl->next_grid_time;
     const unsigned int queued = ctl->queued;
     const int lane_slot = blockIdx.x * B + threadIdx.x;
     const int nslots = gridDim.x * B;
     MT E;
-    if constexpr (SMEM_E) {
+    if constexpr (SMEM_E && PREC == 0) {
         E = MT{smem + threadIdx.x};
     } else {
         E = MT{ebuf + lane_slot, nslots};
@@ -356,48 +539,65 @@ __global__ void __launch_bounds__(B, MINB) k_advance(DevState s, StepCtl* ctl, d
 
     Lane L;
     int cell = -1;
+    int g = 0;               // sub-grid of the lane's cell
+    int cgs = 0;             // its completed global steps
+    double next_grid_time = 0.0;
     bool alive = true;   // lane may still take cells
     bool have = false;   // lane holds a cell
     double y[NEQ], f0[NEQ];
     uint64_t ip = 0;
-    int integrated = 0;
 
     while (__any_sync(0xffffffffu, alive)) {
         // ---- bring the lane to "ready for an attempt"
         while (alive) {
             if (!have) {
-                if (ctl->failure != WR_SUCCESS) { alive = false; break; }
                 const unsigned int q = atomicAdd(&ctl->queue, 1u);
                 if (q >= queued) { alive = false; break; }
                 cell = s.order[q];
-                // advance_collapse_gridwide_kernel prologue, reproducer.cpp:7748-7768
+                g = s.grid_of ? s.grid_of[cell] : 0;
+                const StepCtl* c = ctl + g;
+                if (c->stop || c->failure != WR_SUCCESS) continue;
+                cgs = c->cgs;
                 if (s.steps[cell] != cgs) continue;
                 s.cost[cell] = 0;
-                double xn[NS];
+                double dt_grid;
+                if (s.local_dt == nullptr) {
+                    dt_grid = c->dt_grid;
+                    next_grid_time = c->next_grid_time;
+                    // advance_collapse_gridwide_kernel prologue, reproducer.cpp:7748-7768
+                    double xn[NS];
 #pragma unroll
-                for (int k = 0; k < NS; ++k) xn[k] = s.xn[k * n + cell];
-                const double local_dt = collapse_timestep(xn);
-                if (local_dt < 10.0) continue;
-                const double old_density = s.driver[cell];
-                const double tff = ddiv(local_dt, kTffReduc);
-                const double driver = old_density + dt_grid * ddiv(old_density, tff);
-                s.driver[cell] = driver;
-                if (!valid_positive(driver) || driver > kDriverLimit) continue;
-                const double ratio = ddiv(driver, old_density);
+                    for (int k = 0; k < NS; ++k) xn[k] = s.xn[k * n + cell];
+                    const double local_dt = collapse_timestep(xn);
+                    if (local_dt < 10.0) continue;
+                    const double old_density = s.driver[cell];
+                    const double tff = ddiv(local_dt, kTffReduc);
+                    const double driver = old_density + dt_grid * ddiv(old_density, tff);
+                    s.driver[cell] = driver;
+                    if (!valid_positive(driver) || driver > kDriverLimit) continue;
+                    const double ratio = ddiv(driver, old_density);
 #pragma unroll
-                for (int k = 0; k < NS; ++k) xn[k] *= ratio;
-                const double rho = s.rho[cell] * ratio;
-                // burn_ros2s prologue (reproducer.cpp:7594-7606): e from T
-                const double e = eos_e_from_T(xn, s.T[cell]);
-                // the scaled pre-burn state is what a failed burn leaves behind
-                s.rho[cell] = rho;
-                s.e[cell] = e;
+                    for (int k = 0; k < NS; ++k) xn[k] *= ratio;
+                    const double rho = s.rho[cell] * ratio;
+                    // burn_ros2s prologue (reproducer.cpp:7594-7606): e from T
+                    const double e = eos_e_from_T(xn, s.T[cell]);
+                    // the scaled pre-burn state is what a failed burn leaves behind
+                    s.rho[cell] = rho;
+                    s.e[cell] = e;
 #pragma unroll
-                for (int k = 0; k < NS; ++k) {
-                    s.xn[k * n + cell] = xn[k];
-                    y[k] = xn[k];
+                    for (int k = 0; k < NS; ++k) {
+                        s.xn[k * n + cell] = xn[k];
+                        y[k] = xn[k];
+                    }
+                    y[NS] = e;
+                } else {
+                    // legacy-local: k_prepare_legacy has scaled the cell and set its own dt
+                    dt_grid = s.local_dt[cell];
+                    next_grid_time = s.time[cell] + dt_grid;  // collapse.time += dt, reproducer.cpp:7682
+#pragma unroll
+                    for (int k = 0; k < NS; ++k) y[k] = s.xn[k * n + cell];
+                    y[NS] = s.e[cell];
                 }
-                y[NS] = e;
                 // RODAS::integrate prologue, reproducer.cpp:7218-7235
                 L.tout = dt_grid;
                 L.x = 0.0;
@@ -446,9 +646,9 @@ __global__ void __launch_bounds__(B, MINB) k_advance(DevState s, StepCtl* ctl, d
                     for (int k = 0; k < NS; ++k) s.xn[k * n + cell] = xn[k];
                     s.time[cell] = next_grid_time;
                     s.steps[cell] = cgs + 1;
-                    integrated += 1;
+                    atomicAdd(&ctl[g].integrated, 1);
                 } else {
-                    record_failure(ctl, code);
+                    record_failure(ctl + g, code);
                 }
                 have = false;
                 continue;
@@ -464,11 +664,16 @@ __global__ void __launch_bounds__(B, MINB) k_advance(DevState s, StepCtl* ctl, d
         if (alive && have && L.fresh) {
             double X[NS], T;
             state_from_y(y, X, T);
-            JSink<MT> sink{E, jb, nslots};
-            wr_net_jac_rhs<M>(X, T, f0, sink);
+            if constexpr (PREC == 0) {
+                JSink<MT> sink{E, jb, nslots};
+                wr_net_jac_rhs<M>(X, T, f0, sink);
+            } else {
+                JBackupSink sink{jb, nslots};
+                wr_net_jac_rhs<M>(X, T, f0, sink);
+            }
             L.n_jac += 1;
             L.fresh = false;
-        } else if (alive && have) {
+        } else if (PREC == 0 && alive && have) {
             // retry with the same Jacobian: rebuild E = -J
 #pragma unroll
             for (int r = 0; r < NEQ; ++r)
@@ -479,9 +684,22 @@ __global__ void __launch_bounds__(B, MINB) k_advance(DevState s, StepCtl* ctl, d
         if (alive && have) {
             const double h = L.h;
             const double fac = ddiv(1.0, h * kGamma);
+            int info;
+            if constexpr (PREC == 0) {
 #pragma unroll
-            for (int i = 0; i < NEQ; ++i) E(i, i) = E(i, i) + fac;
-            const int info = lu_decompose(E, ip);
+                for (int i = 0; i < NEQ; ++i) E(i, i) = E(i, i) + fac;
+                info = lu_decompose(E, ip);
+            } else {
+#pragma unroll 1
+                for (int r = 0; r < NEQ; ++r)
+#pragma unroll
+                    for (int c = 0; c < NEQ; ++c) {
+                        double v = -jb[(r * NEQ + c) * nslots];
+                        if (r == c) v = v + fac;
+                        E32(r, c) = __double2float_rn(v);
+                    }
+                info = lu_decompose_f32(E32, ip);
+            }
             if (info != 0) {
                 L.nsing += 1;
                 if (L.nsing >= 5) {
@@ -493,7 +711,7 @@ __global__ void __launch_bounds__(B, MINB) k_advance(DevState s, StepCtl* ctl, d
                         static_cast<uint64_t>(L.n_reject)};
 #pragma unroll
                     for (int k = 0; k < 7; ++k) s.stats[k * n + cell] += st[k];
-                    record_failure(ctl, WR_LU_DECOMPOSITION_ERROR);
+                    record_failure(ctl + g, WR_LU_DECOMPOSITION_ERROR);
                     have = false;
                 } else {
                     L.h = h * 0.5;
@@ -505,7 +723,8 @@ __global__ void __launch_bounds__(B, MINB) k_advance(DevState s, StepCtl* ctl, d
                 double ak1[NEQ], ak2[NEQ], w[NEQ];
 #pragma unroll
                 for (int i = 0; i < NEQ; ++i) ak1[i] = f0[i];
-                lu_solve(E, ip, ak1);
+                if constexpr (PREC == 0) lu_solve(E, ip, ak1);
+                else solve_refined(E32, ip, jb, nslots, fac, ak1);
                 // stages 2 and 3 share one inlined RHS evaluation
 #pragma unroll 1
                 for (int stage = 2; stage <= 3; ++stage) {
@@ -528,7 +747,8 @@ __global__ void __launch_bounds__(B, MINB) k_advance(DevState s, StepCtl* ctl, d
                     wr_net_rhs<M>(X, T, dy);
 #pragma unroll
                     for (int i = 0; i < NEQ; ++i) w[i] += dy[i];
-                    lu_solve(E, ip, w);
+                    if constexpr (PREC == 0) lu_solve(E, ip, w);
+                    else solve_refined(E32, ip, jb, nslots, fac, w);
                     if (stage == 2) {
 #pragma unroll
                         for (int i = 0; i < NEQ; ++i) ak2[i] = w[i];
@@ -581,10 +801,7 @@ __global__ void __launch_bounds__(B, MINB) k_advance(DevState s, StepCtl* ctl, d
             }
         }
     }
-    // integrated count: one atomic per warp
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) integrated += __shfl_xor_sync(0xffffffffu, integrated, off);
-    if ((threadIdx.x & 31) == 0 && integrated) atomicAdd(&ctl->integrated, integrated);
+
 }
 
 }  // namespace wr

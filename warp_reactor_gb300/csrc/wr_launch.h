@@ -15,17 +15,23 @@ constexpr int kPrepareThreads = 256;
 //   0  128 threads x 1 block per SM, iteration matrix in shared memory (225 KiB)
 //   1  128 threads x 2 blocks per SM, iteration matrix in a global lane array
 //   2  256 threads x 1 block per SM, iteration matrix in a global lane array
-constexpr int kAdvanceVariants = 3;
+//   3  precision form: 256 threads x 1 block per SM, FP32 factorisation in shared
+//      memory (900 B per lane) with one FP64 residual refinement per stage solve
+constexpr int kAdvanceVariants = 4;
+constexpr int kPrecisionVariant = 3;
 struct AdvanceShape {
     int threads;
     int blocks_per_sm;
     bool smem_matrix;
+    int precision;  // 0 FP64 factorisation, 1 FP32 factorisation + FP64 refinement
 };
-constexpr AdvanceShape kAdvanceShapes[kAdvanceVariants] = {{128, 1, true}, {128, 2, false}, {256, 1, false}};
+constexpr AdvanceShape kAdvanceShapes[kAdvanceVariants] = {
+    {128, 1, true, 0}, {128, 2, false, 0}, {256, 1, false, 0}, {256, 1, true, 1}};
 
 constexpr size_t advance_smem_bytes(int variant) {
     return kAdvanceShapes[variant].smem_matrix
-               ? static_cast<size_t>(NEQ) * NEQ * kAdvanceShapes[variant].threads * sizeof(double)
+               ? static_cast<size_t>(NEQ) * NEQ * kAdvanceShapes[variant].threads *
+                     (kAdvanceShapes[variant].precision ? sizeof(float) : sizeof(double))
                : 0;
 }
 
