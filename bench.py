@@ -338,6 +338,97 @@ def probe_fp64():
     return 0
 
 
+def diff_form(args):
+    """Differentiation form (--diff): 16^3 reference cells, perturbations on, the
+    plain run's schedule; loss = sum over cells of sum_s w_s (log q_s - log t_s)^2
+    over H2, HD, e- and T with a seeded target; gradients in all 15 inputs per
+    cell and the network's log rate multipliers (seeded N(0, 0.1^2)).  Times the
+    forward map and the adjoint (CUDA events bracket each call; both are
+    synchronous), and checks the adjoint against the CPU tangent-linear and central
+    differences of the frozen map on a sample of cells."""
+    import torch
+    import warp_reactor_gb300 as wr
+    from warp_reactor_gb300 import build, diff
+    from oracle import oracle as O
+    build.build_all()
+    grid = args.diff_grid
+    cells = wr.make_grid(grid)
+    n = len(cells)
+    t0 = time.perf_counter()
+    sched = diff.schedule(cells)
+    plain_s = time.perf_counter() - t0
+    rng = np.random.default_rng(2024)
+    P = diff.num_multipliers()
+    lm = rng.normal(0.0, 0.1, P)
+    sel = [8, 10, 0, 14]  # H2, HD, e-, T
+    cells_dev = torch.from_numpy(np.ascontiguousarray(cells).view(np.uint8)).cuda()
+    u = torch.from_numpy(diff.initial_u(cells)).cuda()
+    lm_dev = torch.from_numpy(lm).cuda()
+    q = torch.empty((n, 15), dtype=torch.float64, device="cuda")
+    with diff.DiffMap(n) as dm:
+        fwd, bwd = [], []
+        for rep in range(2):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            dm.forward(cells_dev, u, lm_dev, sched, True, q)
+            fwd.append(time.perf_counter() - t)
+            qn = q.cpu().numpy()
+            if rep == 0:
+                target = qn[:, sel] * np.exp(rng.normal(0.0, 0.1, (n, len(sel))))
+            qbar = np.zeros((n, 15))
+            qbar[:, sel] = 2.0 * (np.log(qn[:, sel]) - np.log(target)) / qn[:, sel]
+            ubar = torch.empty((n, 15), dtype=torch.float64, device="cuda")
+            pbar = torch.empty(P, dtype=torch.float64, device="cuda")
+            qbar_dev = torch.from_numpy(qbar).cuda()
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            dm.backward(qbar_dev, ubar, pbar)
+            bwd.append(time.perf_counter() - t)
+        hbuf, counts = dm.record()
+        # sample checks: adjoint restricted to the sample cells (seed only there)
+        sample = np.unique(np.concatenate([[0, n - 1], rng.choice(n, 14, replace=False)]))
+        qbar_s = np.zeros_like(qbar)
+        smooth = [8, 0, 14]  # H2, e-, T: well above the absolute tolerance
+        qbar_s[sample[:, None], smooth] = qbar[sample[:, None], smooth]
+        dm.backward(torch.from_numpy(qbar_s).cuda(), ubar, pbar)
+        ubar_s, pbar_s = ubar.cpu().numpy(), pbar.cpu().numpy()
+    D = O.load_diff()
+    sub = cells[sample]
+    ids = sample.astype(np.int32)
+    u_s = diff.initial_u(sub)
+    hb, cn = hbuf[sample], counts[sample]
+    tl_err, fd_err = [], []
+    for trial in range(3):
+        du = np.zeros_like(u_s)
+        du[:, 14] = rng.normal(size=len(sample)) * u_s[:, 14]
+        dp = rng.normal(size=P)
+        _, qs, dq = D.tangent(sub, sched, hb, cn, du=du, dlog_mult=dp, u=u_s, log_mult=lm, cell_ids=ids)
+        tl = (qbar_s[sample] * dq).sum()
+        adj = (ubar_s[sample] * du).sum() + pbar_s @ dp
+        tl_err.append(abs(tl - adj) / max(np.abs(qbar_s[sample] * dq).sum(), 1e-300))
+        eps = 1e-6
+        _, qa = D.replay(sub, sched, hb, cn, u=u_s, log_mult=lm + eps * dp, cell_ids=ids)
+        _, qb = D.replay(sub, sched, hb, cn, u=u_s, log_mult=lm - eps * dp, cell_ids=ids)
+        fd = ((qbar_s[sample] * (qa - qb)).sum()) / (2 * eps)
+        adj_p = pbar_s @ dp
+        fd_err.append(abs(fd - adj_p) / max(abs(fd), 1e-300))
+    acc = counts.sum(1)
+    line = {
+        "form": "differentiation", "grid": grid, "cells": n, "outer_steps": len(sched),
+        "multipliers": P, "loss_species": ["H2", "HD", "e-", "T"],
+        "forward_s": min(fwd), "adjoint_s": min(bwd), "adjoint_over_forward": min(bwd) / min(fwd),
+        "forward_cells_per_s": n / min(fwd), "plain_run_with_schedule_s": plain_s,
+        "accepted_steps_per_cell": {"min": int(acc.min()), "median": float(np.median(acc)), "max": int(acc.max())},
+        "checkpoints": "outer-step states (18 doubles per cell per step) + burn checkpoints every 32 accepted steps",
+        "check_sample_cells": int(len(sample)),
+        "adjoint_vs_tangent_linear_max_rel": float(max(tl_err)),
+        "adjoint_vs_central_fd_max_rel": float(max(fd_err)), "fd_h": 1e-6,
+        "grad_norm_u": float(np.linalg.norm(ubar_s)), "grad_norm_p": float(np.linalg.norm(pbar_s)),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def profile_steps(args):
     """A short, fixed run for ncu: ``--profile-steps S`` outer steps of the grid
     through wr_prepare / wr_advance (the same kernels as wr_run)."""
@@ -375,11 +466,16 @@ def main():
     ap.add_argument("--no-forms", action="store_true", help="skip the precision-form run")
     ap.add_argument("--probe-fp64", action="store_true",
                     help="print this GPU's FP64 issue interval per warp count and the FMA peak, exit")
+    ap.add_argument("--diff", action="store_true",
+                    help="differentiation form: time forward and adjoint on a --diff-grid^3 grid, check gradients")
+    ap.add_argument("--diff-grid", type=int, default=16)
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiling driver: run this many outer steps host-stepped, print nothing, exit")
     args = ap.parse_args()
     if args.probe_fp64:
         return probe_fp64()
+    if args.diff:
+        return diff_form(args)
     if args.profile_steps > 0:
         return profile_steps(args)
     if args.warmup < 3:

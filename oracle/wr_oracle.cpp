@@ -354,6 +354,9 @@ int ros2s_integrate(double* y, double tout, double dt0, Counters& c) {
             last = false;
             h = hnew;
             if (n_accept >= 1) c.n_reject += 1;
+            // the reject loop has no exit of its own: a step size that underflowed
+            // to zero ends the burn with DT_UNDERFLOW (the GPU library does the same)
+            if (hnew == 0.0) return WR_DT_UNDERFLOW;
         }
     }
 }

@@ -264,10 +264,13 @@ def run_cells(cells: np.ndarray, perturb: bool = True, math: int = MATH_PORTABLE
     return rc, cgs
 
 
-def make_batch_grid(grid_id: int, num_cells: int, sigma_dex: float = 1.0, log10_tmin: float = 1.5,
+def make_batch_grid(grid_id: int, num_cells: int, sigma_dex: float = 1.0, log10_tmin: float = 2.0,
                     log10_tmax: float = 4.0) -> np.ndarray:
     """Seeded cells of the batching workload (``wr_make_batch_state``): log-normal
-    density (sigma in dex) and log-uniform temperature."""
+    density (sigma in dex) and log-uniform temperature.  The temperature range
+    starts at 100 K: below it the reference's analytic Jacobian evaluates to NaN
+    (rate fits outside their range), and the reference integrator's reject loop
+    never accepts a step."""
     out = np.zeros(int(num_cells), COLLAPSE_STATE)
     L = lib()
     for i in range(int(num_cells)):

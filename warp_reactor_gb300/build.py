@@ -35,6 +35,9 @@ NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompil
 CXX_FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fPIC"]
 
 CUDA_UNITS = ["wr_capi.cu", "wr_adv_portable.cu", "wr_adv_cuda.cu", "wr_diag.cu"]
+# differentiation form: relocatable device code, device-linked into one object
+# (its generated derivative code is split over several units that compile in parallel)
+RDC_UNITS = ["wr_diff.cu", "wr_diff_bwd.cu", "wr_diff_net.cu", "wr_diff_jvjp0.cu", "wr_diff_jvjp1.cu"]
 
 
 def _nvcc() -> str:
@@ -80,17 +83,25 @@ def build_library(verbose=False, jobs=None) -> str:
     headers = _headers()
     objs = []
     tasks = []
-    for unit in CUDA_UNITS:
+    rdc_objs = []
+    for unit in CUDA_UNITS + RDC_UNITS:
         src = os.path.join(CSRC, unit)
         obj = os.path.join(OUT, unit.replace(".cu", ".o"))
-        objs.append(obj)
+        rdc = unit in RDC_UNITS
+        (rdc_objs if rdc else objs).append(obj)
         if _stale(obj, [src] + headers):
-            tasks.append([nvcc] + NVCC_FLAGS + ["-c", src, "-o", obj])
-    with cf.ThreadPoolExecutor(max_workers=jobs or len(CUDA_UNITS)) as ex:
+            tasks.append([nvcc] + NVCC_FLAGS + (["-rdc=true"] if rdc else []) + ["-c", src, "-o", obj])
+    # longest units first
+    tasks.sort(key=lambda c: 0 if any(u in c[-3] for u in ("jvjp", "bwd", "net")) else 1)
+    with cf.ThreadPoolExecutor(max_workers=jobs or len(CUDA_UNITS) + len(RDC_UNITS)) as ex:
         list(ex.map(lambda c: _run(c, verbose), tasks))
+    dlink = os.path.join(OUT, "wr_diff_dlink.o")
+    if _stale(dlink, rdc_objs):
+        _run([nvcc] + ARCH + ["-dlink", "-Xcompiler", "-fPIC", "-o", dlink] + rdc_objs, verbose)
     lib = os.path.join(OUT, "libwarp_reactor.so")
-    if _stale(lib, objs):
-        _run([nvcc] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"], verbose)
+    all_objs = objs + rdc_objs + [dlink]
+    if _stale(lib, all_objs):
+        _run([nvcc] + ARCH + ["-shared", "-o", lib] + all_objs + ["-lcudart"], verbose)
     return lib
 
 
@@ -119,7 +130,13 @@ def build_oracle(verbose=False) -> list:
         outs.append(so)
         if _stale(so, deps):
             tasks.append(["g++"] + CXX_FLAGS + ["-fopenmp", "-shared"] + defs + ["-o", so, src])
-    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+    # the differentiation form's map and tangent-linear (portable math)
+    dsrc = os.path.join(ORACLE, "wr_oracle_diff.cpp")
+    dso = os.path.join(ORACLE_OUT, "libwr_oracle_diff.so")
+    outs.append(dso)
+    if _stale(dso, deps + [dsrc, os.path.join(CSRC, "generated", "network_adj.h")]):
+        tasks.append(["g++"] + CXX_FLAGS + ["-fopenmp", "-shared", "-o", dso, dsrc])
+    with cf.ThreadPoolExecutor(max_workers=3) as ex:
         list(ex.map(lambda c: _run(c, verbose), tasks))
     return outs
 

@@ -797,6 +797,23 @@ __global__ void __launch_bounds__(B, MINB) k_advance(DevState s, StepCtl* ctl, d
                     L.last = false;
                     L.h = hnew;
                     if (L.n_accept >= 1) L.n_reject += 1;
+                    if (hnew == 0.0) {
+                        // The step size has underflowed inside the reject loop, which
+                        // has no exit of its own (reproducer.cpp:7259-7345 leaves it
+                        // only on an accepted attempt): with a NaN error norm (the
+                        // network is undefined below ~100 K) it would retry forever.
+                        // A zero step is the reference's DT_UNDERFLOW (:7240), so the
+                        // cell ends with that code here instead of never ending.
+                        const uint64_t st[7] = {
+                            static_cast<uint64_t>(L.n_step), static_cast<uint64_t>(3 * L.n_step),
+                            static_cast<uint64_t>(L.n_jac), static_cast<uint64_t>(L.n_decomp),
+                            static_cast<uint64_t>(3 * L.n_step), static_cast<uint64_t>(L.n_accept),
+                            static_cast<uint64_t>(L.n_reject)};
+#pragma unroll
+                        for (int k = 0; k < 7; ++k) s.stats[k * n + cell] += st[k];
+                        record_failure(ctl + g, WR_DT_UNDERFLOW);
+                        have = false;
+                    }
                 }
             }
         }

@@ -5,8 +5,9 @@
     ``network.ir`` (needs the reference tree; run once, the IR is committed);
 
 ``python -m warp_reactor_gb300.gen.build_network emit [out.h]``
-    writes ``csrc/generated/network_gen.h`` from the committed ``network.ir``
-    (run by the package build on every machine);
+    writes ``csrc/generated/network_gen.h`` and ``csrc/generated/network_adj.h``
+    (derivative code, ``adjoint.py``) from the committed ``network.ir`` (run by
+    the package build on every machine);
 
 ``python -m warp_reactor_gb300.gen.build_network counts``
     prints the source-level and CSE'd operation counts.
@@ -16,11 +17,13 @@ from __future__ import annotations
 import os
 import sys
 
+from . import adjoint as _adjoint
 from . import emit as _emit
 from . import ir_io
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 DEFAULT_HEADER = os.path.join(os.path.dirname(HERE), "csrc", "generated", "network_gen.h")
+ADJOINT_HEADER = os.path.join(os.path.dirname(HERE), "csrc", "generated", "network_adj.h")
 
 IR_HEADER = """\
 14-species primordial network (H/He/D, energy equation), RHS and analytic Jacobian.
@@ -48,17 +51,25 @@ def op_counts(dag):
     }
 
 
-def emit_header(out_path: str = DEFAULT_HEADER, ir_path: str = ir_io.DEFAULT_PATH) -> str:
-    dag = ir_io.load(ir_path)
-    text = _emit.emit_header(dag, ir_io.digest(ir_path))
-    os.makedirs(os.path.dirname(out_path), exist_ok=True)
+def _write_if_changed(path: str, text: str) -> None:
+    os.makedirs(os.path.dirname(path), exist_ok=True)
     old = None
-    if os.path.exists(out_path):
-        with open(out_path) as f:
+    if os.path.exists(path):
+        with open(path) as f:
             old = f.read()
     if old != text:
-        with open(out_path, "w") as f:
+        with open(path, "w") as f:
             f.write(text)
+
+
+def emit_header(out_path: str = DEFAULT_HEADER, ir_path: str = ir_io.DEFAULT_PATH,
+                adjoint_path: str = ADJOINT_HEADER) -> str:
+    """Write the network header and, beside it, the derivative code of the
+    differentiation form (``network_adj.h``)."""
+    dag = ir_io.load(ir_path)
+    digest = ir_io.digest(ir_path)
+    _write_if_changed(out_path, _emit.emit_header(dag, digest))
+    _write_if_changed(adjoint_path, _adjoint.emit_header(dag, digest))
     return out_path
 
 
