@@ -191,6 +191,26 @@ int wr_get_run_timing(wr_ctx* ctx, wr_run_timing* out);
 int wr_run_cells(wr_collapse_state* cells, int num_cells, int perturb,
                  int* completed_global_steps);
 
+/* No-allocation advance.  Some callers cannot allocate device memory: they keep
+ * their cells in device buffers owned by another framework's allocator or pool,
+ * or run on a device whose memory is budgeted for them.  This entry point runs
+ * one advance step (the same result as wr_advance on those cells) on
+ * num_cells <= WR_NOALLOC_MAX_CELLS records in the caller's device memory,
+ * updated in place, and allocates nothing: its scratch is one fixed file-scope
+ * device array (7.9 MiB, resident on every GPU that loads the library until the
+ * process exits).  Calls share that array, so calls that overlap on the GPU race;
+ * issue them one at a time.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) and must come before any stream capture.
+ * It runs on the legacy default stream and returns after the step completes,
+ * with *integrated_out = cells committed.  No counterpart in the reference. */
+#define WR_NOALLOC_MAX_CELLS 4096
+#define WR_NOALLOC_LANES 4096
+int wr_advance_cells_noalloc(wr_collapse_state* d_cells, int num_cells, int completed_global_steps,
+                             double next_grid_time, double dt_grid, int* integrated_out);
+
+/* Text of the last error of wr_advance_cells_noalloc on this host thread. */
+const char* wr_noalloc_last_error(void);
+
 /* The reference's initial collapse cell (make_collapse_state,
  * reproducer.cpp:7533-7546). */
 void wr_make_collapse_state(wr_collapse_state* out);
