@@ -175,13 +175,14 @@ int wr_set_profiling(wr_ctx* ctx, int on);
  *   3  the precision form: 256 lanes per SM, the iteration matrix factorised in
  *      FP32 with one FP64-residual refinement sweep per stage solve; RHS,
  *      exp/log, stage combination, error norm, controller and EOS stay FP64
- * Variants 0-2 give identical results (only the speed differs); variant 3
+ *   4  384 lanes per SM (1 block), iteration matrix in global memory
+ * Variants 0-2 and 4 give identical results (only the speed differs); variant 3
  * approximates the FP64 result.  No reference
  * counterpart (the reference fixes 128 threads per block, reproducer.cpp:7398). */
 int wr_set_advance_variant(wr_ctx* ctx, int variant);
 
 /* Autotuner: times the first `steps` outer steps of the uploaded state with each
- * exact launch shape (variants 0-2), restores the state, selects the fastest and
+ * exact launch shape (variants 0-2 and 4), restores the state, selects the fastest and
  * returns it in *best_variant.  The precision form is never chosen by it. */
 int wr_autotune(wr_ctx* ctx, int perturb, int steps, int* best_variant);
 int wr_get_run_timing(wr_ctx* ctx, wr_run_timing* out);

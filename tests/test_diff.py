@@ -149,11 +149,15 @@ def test_gpu_forward_bitwise(wr, gpu, diff_oracle, grid2):
         dm.forward(cells_dev, None, None, hist, True, q)
         qp = np.concatenate([plain["xn"], plain["T"][:, None]], 1)
         assert q.cpu().numpy().tobytes() == qp.tobytes()
+        # random multipliers over the first 300 outer steps (with this grid's
+        # schedule, the thermally unstable cell 1 ends in the reference
+        # controller's DT_UNDERFLOW near step 690 for such draws, on the CPU too)
+        h = hist[:300]
         lm = np.random.default_rng(3).normal(0, 0.1, dm.num_multipliers)
         lm_dev = torch.from_numpy(lm).cuda()
-        dm.forward(cells_dev, None, lm_dev, hist, True, q)
+        dm.forward(cells_dev, None, lm_dev, h, True, q)
         hbuf, counts = dm.record()
-    rc, qo, hbo, co = diff_oracle.record(cells, hist, log_mult=lm, cap=hbuf.shape[1])
+    rc, qo, hbo, co = diff_oracle.record(cells, h, log_mult=lm, cap=hbuf.shape[1])
     assert rc == 1
     assert (counts == co).all()
     assert hbuf.tobytes() == hbo.tobytes()
@@ -171,7 +175,8 @@ def test_gpu_adjoint_against_tangent_linear(wr, gpu, diff_oracle, grid2, nsteps)
     h = hist[:nsteps]
     n = len(cells)
     rng = np.random.default_rng(nsteps)
-    lm = rng.normal(0, 0.1, diff_oracle.num_multipliers)
+    # the whole schedule at p = 0 (see test_gpu_forward_bitwise), 100 steps at random p
+    lm = rng.normal(0, 0.1, diff_oracle.num_multipliers) if nsteps <= 100 else np.zeros(diff_oracle.num_multipliers)
     u = diff.initial_u(cells)
     cells_dev = _device_setup(wr, cells, torch)
     q = torch.empty((n, 15), dtype=torch.float64, device="cuda")

@@ -21,6 +21,9 @@ cudaError_t launch_advance_portable(int variant, int blocks, cudaStream_t stream
         case 2:
             k_advance<PortableMathCall, 256, 1, false><<<blocks, 256, 0, stream>>>(s, ctl, jbackup, ebuf);
             break;
+        case 4:
+            k_advance<PortableMathCall, 384, 1, false><<<blocks, 384, 0, stream>>>(s, ctl, jbackup, ebuf);
+            break;
         case 3:
             k_advance<PortableMathCall, 256, 1, true, 1>
                 <<<blocks, 256, advance_smem_bytes(kPrecisionVariant), stream>>>(s, ctl, jbackup, ebuf);

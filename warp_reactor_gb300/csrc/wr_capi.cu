@@ -663,7 +663,8 @@ int wr_autotune(wr_ctx* ctx, int perturb, int steps, int* best_variant) {
     int best = keep;
     // candidates: the exact (FP64) launch shapes; the precision form is a
     // different arithmetic and is chosen explicitly, never by the tuner
-    for (int v = 0; e == cudaSuccess && rc == WR_SUCCESS && v < kPrecisionVariant; ++v) {
+    for (int v = 0; e == cudaSuccess && rc == WR_SUCCESS && v < kAdvanceVariants; ++v) {
+        if (v == kPrecisionVariant) continue;
         e = cudaMemcpyAsync(ctx->state_buf, snap, bytes, cudaMemcpyDeviceToDevice, ctx->stream);
         if (e != cudaSuccess) break;
         rc = reset_ctl(ctx) == cudaSuccess ? WR_SUCCESS : WR_BAD_INPUTS;

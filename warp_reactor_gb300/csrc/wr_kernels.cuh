@@ -121,6 +121,42 @@ struct PortableMathCall {
     static __device__ __forceinline__ double div(double a, double b) { return wr_div_call(a, b); }
 };
 
+// Batched out-of-line exp/log: the generated network evaluates up to four
+// independent exp (log) in one call; inlined side by side, the four integer
+// chains interleave, so a warp has four independent instructions ready where one
+// chain would stall on its own latency.
+static __device__ __noinline__ WrD2 wr_exp2_call(double a, double b) { return {wr_exp(a), wr_exp(b)}; }
+static __device__ __noinline__ WrD3 wr_exp3_call(double a, double b, double c) {
+    return {wr_exp(a), wr_exp(b), wr_exp(c)};
+}
+static __device__ __noinline__ WrD4 wr_exp4_call(double a, double b, double c, double d) {
+    return {wr_exp(a), wr_exp(b), wr_exp(c), wr_exp(d)};
+}
+static __device__ __noinline__ WrD2 wr_log2_call(double a, double b) { return {wr_log(a), wr_log(b)}; }
+static __device__ __noinline__ WrD3 wr_log3_call(double a, double b, double c) {
+    return {wr_log(a), wr_log(b), wr_log(c)};
+}
+static __device__ __noinline__ WrD4 wr_log4_call(double a, double b, double c, double d) {
+    return {wr_log(a), wr_log(b), wr_log(c), wr_log(d)};
+}
+}  // namespace wr
+
+template <>
+struct WrBatch<wr::PortableMathCall> {
+    static __device__ __forceinline__ WrD2 exp2(double a, double b) { return wr::wr_exp2_call(a, b); }
+    static __device__ __forceinline__ WrD3 exp3(double a, double b, double c) { return wr::wr_exp3_call(a, b, c); }
+    static __device__ __forceinline__ WrD4 exp4(double a, double b, double c, double d) {
+        return wr::wr_exp4_call(a, b, c, d);
+    }
+    static __device__ __forceinline__ WrD2 log2(double a, double b) { return wr::wr_log2_call(a, b); }
+    static __device__ __forceinline__ WrD3 log3(double a, double b, double c) { return wr::wr_log3_call(a, b, c); }
+    static __device__ __forceinline__ WrD4 log4(double a, double b, double c, double d) {
+        return wr::wr_log4_call(a, b, c, d);
+    }
+};
+
+namespace wr {
+
 
 // ------------------------------------------------------------------ prepare
 __device__ __forceinline__ void record_failure(StepCtl* ctl, int code) {

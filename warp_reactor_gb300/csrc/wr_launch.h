@@ -17,7 +17,9 @@ constexpr int kPrepareThreads = 256;
 //   2  256 threads x 1 block per SM, iteration matrix in a global lane array
 //   3  precision form: 256 threads x 1 block per SM, FP32 factorisation in shared
 //      memory (900 B per lane) with one FP64 residual refinement per stage solve
-constexpr int kAdvanceVariants = 4;
+//   4  384 threads x 1 block per SM (at most 168 registers per thread: more spills,
+//      twelve warps per SM to hide them)
+constexpr int kAdvanceVariants = 5;
 constexpr int kPrecisionVariant = 3;
 struct AdvanceShape {
     int threads;
@@ -26,7 +28,7 @@ struct AdvanceShape {
     int precision;  // 0 FP64 factorisation, 1 FP32 factorisation + FP64 refinement
 };
 constexpr AdvanceShape kAdvanceShapes[kAdvanceVariants] = {
-    {128, 1, true, 0}, {128, 2, false, 0}, {256, 1, false, 0}, {256, 1, true, 1}};
+    {128, 1, true, 0}, {128, 2, false, 0}, {256, 1, false, 0}, {256, 1, true, 1}, {384, 1, false, 0}};
 
 constexpr size_t advance_smem_bytes(int variant) {
     return kAdvanceShapes[variant].smem_matrix
