@@ -38,7 +38,7 @@ int wr_diff_num_multipliers(void);
 /* Context for num_cells cells, schedules of up to max_outer_steps steps and up to
  * max_accepted_per_cell accepted ROS2S steps per cell over the whole schedule
  * (a cell that needs more fails with WR_TOO_MANY_STEPS).  Device memory:
- * 8*(18*max_outer_steps + 1.03*max_accepted_per_cell + 600) + 5*max_outer_steps
+ * 8*(18*max_outer_steps + 1.03*max_accepted_per_cell + 9600) + 5*max_outer_steps
  * bytes per cell.  NULL on bad sizes or allocation failure. */
 wr_diff* wr_diff_create(int num_cells, int max_outer_steps, int max_accepted_per_cell, int device);
 void wr_diff_destroy(wr_diff* d);

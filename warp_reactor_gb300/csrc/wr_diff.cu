@@ -141,7 +141,7 @@ static __device__ __noinline__ int burn_record(double* y, double tout, const dou
 }
 
 // one accepted step of the frozen controller
-__device__ void step_replay(double* y, double h, const double* mult) {
+__device__ void step_replay(double* y, double h, const double* mult, double* st) {
     double Jm[NEQ * NEQ], Em[NEQ * NEQ];
     MatL E{Em};
     uint64_t ip = 0;
@@ -151,6 +151,18 @@ __device__ void step_replay(double* y, double h, const double* mult) {
     net_jac(X, T, Jm);
     factor(Jm, h, E, ip);
     ros2s_stages(y, h, E, ip, mult, ak1, ak2, ak3, ynew, work);
+    if (st != nullptr) {
+        // what the step's adjoint needs: the factorised matrix, pivots, stage vectors
+#pragma unroll 1
+        for (int k = 0; k < NEQ * NEQ; ++k) st[k] = Em[k];
+        st[kStageIp] = __longlong_as_double(static_cast<long long>(ip));
+#pragma unroll
+        for (int i = 0; i < NEQ; ++i) {
+            st[kStageK1 + i] = ak1[i];
+            st[kStageK2 + i] = ak2[i];
+            st[kStageK3 + i] = ak3[i];
+        }
+    }
 #pragma unroll
     for (int i = 0; i < NEQ; ++i) y[i] = ynew[i];
 }
@@ -239,6 +251,7 @@ struct wr_diff {
     double* hbuf = nullptr;
     double* segck = nullptr;
     double* ys = nullptr;
+    double* stage = nullptr;
     double* mbar = nullptr;
     double* mult = nullptr;
     double* dt_hist = nullptr;
@@ -278,6 +291,7 @@ wr::diff::Args make_args(wr_diff* d) {
     a.hbuf = d->hbuf;
     a.segck = d->segck;
     a.ys = d->ys;
+    a.stage = d->stage;
     a.mbar = d->mbar;
     a.status = d->status;
     return a;
@@ -307,6 +321,7 @@ wr_diff* wr_diff_create(int num_cells, int max_outer_steps, int max_accepted_per
               cuda_ok(d, cudaMalloc(&d->hbuf, n * d->cap * sizeof(double)), "cudaMalloc") &&
               cuda_ok(d, cudaMalloc(&d->segck, n * d->nseg * wr::NEQ * sizeof(double)), "cudaMalloc") &&
               cuda_ok(d, cudaMalloc(&d->ys, n * wr::diff::kSeg * wr::NEQ * sizeof(double)), "cudaMalloc") &&
+              cuda_ok(d, cudaMalloc(&d->stage, n * wr::diff::kSeg * wr::diff::kStage * sizeof(double)), "cudaMalloc") &&
               cuda_ok(d, cudaMalloc(&d->mbar, n * wr::diff::NP * sizeof(double)), "cudaMalloc") &&
               cuda_ok(d, cudaMalloc(&d->mult, wr::diff::NP * sizeof(double)), "cudaMalloc") &&
               cuda_ok(d, cudaMalloc(&d->dt_hist, S * sizeof(double)), "cudaMalloc") &&
@@ -327,6 +342,7 @@ void wr_diff_destroy(wr_diff* d) {
     cudaFree(d->hbuf);
     cudaFree(d->segck);
     cudaFree(d->ys);
+    cudaFree(d->stage);
     cudaFree(d->mbar);
     cudaFree(d->mult);
     cudaFree(d->dt_hist);

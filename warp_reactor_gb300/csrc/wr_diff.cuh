@@ -41,6 +41,7 @@
 //   hbuf   [n][cap]     accepted step sizes in order, one row per cell
 //   segck  [n][cap/32+1][15]   burn-segment checkpoints (backward scratch)
 //   ys     [n][32][15]  states of the segment being reversed (backward scratch)
+//   stage  [n][32][271] LU, pivots and stage vectors of those steps (backward scratch)
 //   mbar   [n][P]       per-cell multiplier adjoints
 //
 // Source files: wr_diff.cu (forward kernel, C ABI), wr_diff_bwd.cu (adjoint
@@ -65,6 +66,12 @@ constexpr int NP = 44;        // rate-coefficient multipliers (WR_NUM_RATE_MULT,
 constexpr int kFields = 18;   // xn[14], T, e, rho, driver
 constexpr int kSeg = 32;      // accepted steps between burn checkpoints
 constexpr int kThreads = 32;  // one warp per block: a small grid spreads over all SMs
+// per-step record of the adjoint's segment pass: LU (225), pivots (1), k1, k2, k3
+constexpr int kStageIp = NEQ * NEQ;
+constexpr int kStageK1 = kStageIp + 1;
+constexpr int kStageK2 = kStageK1 + NEQ;
+constexpr int kStageK3 = kStageK2 + NEQ;
+constexpr int kStage = kStageK3 + NEQ;
 
 using M = PortableMath;
 
@@ -102,6 +109,7 @@ struct Args {
     double* ubar;           // [n][15]
     double* segck;
     double* ys;
+    double* stage;          // [n][32][kStage]
     double* mbar;           // [n][P]
 };
 
@@ -109,7 +117,9 @@ struct Args {
 __device__ void ros2s_stages(const double* y, double h, MatL E, uint64_t ip, const double* mult, double* ak1,
                              double* ak2, double* ak3, double* ynew, double* work);
 __device__ int factor(const double* J, double h, MatL E, uint64_t& ip);
-__device__ void step_replay(double* y, double h, const double* mult);
+// one accepted step of the frozen controller; with st != nullptr it also stores
+// the step's factorised iteration matrix, pivots and stage vectors (kStage doubles)
+__device__ void step_replay(double* y, double h, const double* mult, double* st);
 
 __global__ void k_diff_forward(Args a);
 __global__ void k_diff_backward(Args a);

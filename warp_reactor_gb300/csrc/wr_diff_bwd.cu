@@ -128,18 +128,15 @@ static __device__ __noinline__ void rhs_adj_at(const double* ys, const double* m
 
 // Adjoint of one accepted step y -> ynew with step h: lam (in: adjoint of ynew,
 // out: adjoint of y); multiplier adjoints accumulate into mbar.
-static __device__ __noinline__ void step_adj(const double* y, double h, const double* mult, double* lam, double* mbar) {
-    double Em[NEQ * NEQ], Jb[NEQ * NEQ];
-    MatL E{Em};
-    uint64_t ip = 0;
-    double k1[NEQ], k2[NEQ], k3[NEQ], ynew[NEQ], work[NEQ];
-    {
-        double X[NS], T;
-        state_from_y(y, X, T);
-        net_jac(X, T, Jb);  // J, then the matrix is factorised and Jb reused as Jbar
-        factor(Jb, h, E, ip);
-    }
-    ros2s_stages(y, h, E, ip, mult, k1, k2, k3, ynew, work);
+static __device__ __noinline__ void step_adj(const double* y, double h, const double* mult, double* lam,
+                                             double* mbar, double* st) {
+    // the step's factorised matrix, pivots and stage vectors, stored by its replay
+    MatL E{st};
+    const uint64_t ip = static_cast<uint64_t>(__double_as_longlong(st[kStageIp]));
+    const double* k1 = st + kStageK1;
+    const double* k2 = st + kStageK2;
+    const double* k3 = st + kStageK3;
+    double Jb[NEQ * NEQ];
     double yb[NEQ], kb1[NEQ], kb2[NEQ], r[NEQ], ys[NEQ];
 #pragma unroll
     for (int i = 0; i < NEQ; ++i) {
@@ -212,34 +209,50 @@ static __device__ __noinline__ void step_adj(const double* y, double h, const do
 }
 
 // Burn replay for the adjoint: the state at the start of every 32-step segment
-// into segck, the burn's final state into y (y holds y0 on entry).
-static __device__ __noinline__ void burn_checkpoint(double* y, const double* hs, int count, const double* mult, double* segck) {
+// into segck, the states before each step of the last segment into ys, the
+// burn's final state into y (y holds y0 on entry).
+static __device__ __noinline__ void burn_checkpoint(double* y, const double* hs, int count, const double* mult,
+                                                    double* segck, double* ys, double* stage) {
     const int nseg = (count + kSeg - 1) / kSeg;
     for (int g = 0; g < nseg; ++g) {
 #pragma unroll
         for (int i = 0; i < NEQ; ++i) segck[g * NEQ + i] = y[i];
-        const int k1 = (g * kSeg + kSeg < count) ? g * kSeg + kSeg : count;
-        for (int k = g * kSeg; k < k1; ++k) step_replay(y, hs[k], mult);
+        const int k0 = g * kSeg;
+        const int k1 = (k0 + kSeg < count) ? k0 + kSeg : count;
+        for (int k = k0; k < k1; ++k) {
+            // the last segment's states and step records go straight to ys and
+            // stage: it is reversed first
+            const bool last = g == nseg - 1;
+            if (last) {
+#pragma unroll
+                for (int i = 0; i < NEQ; ++i) ys[(k - k0) * NEQ + i] = y[i];
+            }
+            step_replay(y, hs[k], mult, last ? stage + static_cast<size_t>(k - k0) * kStage : nullptr);
+        }
     }
 }
 
 // Adjoint of the burn recorded by burn_checkpoint: lam in (adjoint of the final
-// state) / out (adjoint of y0); each segment is recomputed into ys and reversed.
-static __device__ __noinline__ void burn_reverse(const double* hs, int count, const double* mult, double* lam, double* mbar,
-                             const double* segck, double* ys) {
+// state) / out (adjoint of y0); each segment but the last (already in ys) is
+// recomputed into ys from its checkpoint, then reversed step by step.
+static __device__ __noinline__ void burn_reverse(const double* hs, int count, const double* mult, double* lam,
+                                                 double* mbar, const double* segck, double* ys, double* stage) {
     const int nseg = (count + kSeg - 1) / kSeg;
     double y[NEQ];
     for (int g = nseg - 1; g >= 0; --g) {
         const int k0 = g * kSeg;
         const int k1 = (k0 + kSeg < count) ? k0 + kSeg : count;
+        if (g != nseg - 1) {
 #pragma unroll
-        for (int i = 0; i < NEQ; ++i) y[i] = segck[g * NEQ + i];
-        for (int k = k0; k < k1; ++k) {
+            for (int i = 0; i < NEQ; ++i) y[i] = segck[g * NEQ + i];
+            for (int k = k0; k < k1; ++k) {
 #pragma unroll
-            for (int i = 0; i < NEQ; ++i) ys[(k - k0) * NEQ + i] = y[i];
-            if (k + 1 < k1) step_replay(y, hs[k], mult);
+                for (int i = 0; i < NEQ; ++i) ys[(k - k0) * NEQ + i] = y[i];
+                step_replay(y, hs[k], mult, stage + static_cast<size_t>(k - k0) * kStage);
+            }
         }
-        for (int k = k1 - 1; k >= k0; --k) step_adj(ys + (k - k0) * NEQ, hs[k], mult, lam, mbar);
+        for (int k = k1 - 1; k >= k0; --k)
+            step_adj(ys + (k - k0) * NEQ, hs[k], mult, lam, mbar, stage + static_cast<size_t>(k - k0) * kStage);
     }
 }
 
@@ -253,6 +266,7 @@ __global__ void __launch_bounds__(kThreads) k_diff_backward(Args a) {
     double* hrow = a.hbuf + static_cast<size_t>(i) * a.cap;
     double* segck = a.segck + static_cast<size_t>(i) * a.nseg * NEQ;
     double* ys = a.ys + static_cast<size_t>(i) * kSeg * NEQ;
+    double* stage = a.stage + static_cast<size_t>(i) * kSeg * kStage;
     double* mbar = a.mbar + static_cast<size_t>(i) * NP;
     for (int r = 0; r < NP; ++r) mbar[r] = 0.0;
     CellAdj L;
@@ -327,7 +341,7 @@ __global__ void __launch_bounds__(kThreads) k_diff_backward(Args a) {
                 double yN[NEQ];
 #pragma unroll
                 for (int k = 0; k < NEQ; ++k) yN[k] = y0[k];
-                burn_checkpoint(yN, hrow + hbeg, cnt, a.mult, segck);
+                burn_checkpoint(yN, hrow + hbeg, cnt, a.mult, segck, ys, stage);
                 // commit: xd = renormalize(yN, rho2), e3 = yN[14], T3 = eos_re(xd, e3)
                 double xd[NS];
 #pragma unroll
@@ -341,7 +355,7 @@ __global__ void __launch_bounds__(kThreads) k_diff_backward(Args a) {
                 lrho2 = L.rho;
                 renorm_adj(yN, c2.rho, lxd, lam, lrho2);
                 lam[NS] = le3;
-                burn_reverse(hrow + hbeg, cnt, a.mult, lam, mbar, segck, ys);
+                burn_reverse(hrow + hbeg, cnt, a.mult, lam, mbar, segck, ys, stage);
                 // y0 = (xc, e2), e2 = eos_rt(xc, T1), xc = x1 * ratio, rho2 = rho1 * ratio
                 double lratio = 0.0;
 #pragma unroll
