@@ -145,7 +145,7 @@ def algorithmic_ops(cells):
     return nj * f_j + na * f_att, {"F_J": f_j, "F_RHS": f_rhs, "F_attempt": f_att, "jacobians": nj, "attempts": na}
 
 
-def precision_form(wr, device, math_mode, grid=16, steps=40):
+def precision_form(wr, device, math_mode, grid=16, steps=300):
     """The precision form (advance variant 3: FP32 factorisation + one FP64 residual
     refinement per stage solve) next to the plain FP64 form on the first ``steps``
     outer steps of a ``grid``^3 collapse (host-stepped wr_prepare / wr_advance, wall

@@ -221,19 +221,20 @@ def test_precision_form_against_fp64_oracle(wr, gpu, oracle_port):
     times more attempts; that is measured by bench.py, not asserted here.)"""
     cells = wr.make_grid(2)
     ref = oracle_port.make_grid(2)
-    gt, cgs = 0.0, 0
+    gt, gt_o, cgs = 0.0, 0.0, 0
     with wr.Context(len(cells)) as ctx:
         ctx.set_variant(3)
         ctx.upload(cells)
         for step in range(20):
             rc, dt = ctx.prepare(cgs, gt, step, True)
-            rc_o, dt_o = oracle_port.prepare(ref, cgs, gt, step, True)
+            rc_o, dt_o = oracle_port.prepare(ref, cgs, gt_o, step, True)
             assert rc == rc_o == wr.SUCCESS
             assert abs(dt / dt_o - 1) < 1e-9
             rc, cnt = ctx.advance(cgs, gt + dt, dt)
-            rc_o, cnt_o = oracle_port.advance(ref, cgs, gt + dt_o, dt_o)
+            rc_o, cnt_o = oracle_port.advance(ref, cgs, gt_o + dt_o, dt_o)
             assert rc == rc_o == wr.SUCCESS and cnt == cnt_o
             gt += dt
+            gt_o += dt_o
             cgs += 1
         ctx.download(cells)
     rT = np.abs(cells["T"] - ref["T"]) / ref["T"]

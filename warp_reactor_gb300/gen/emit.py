@@ -95,6 +95,11 @@ def schedule(dag: Dag, roots) -> list:
 BATCH_OPS = ("exp", "log")
 BATCH_MAX = 4
 BATCH_WINDOW = 256
+# Batched exp/log calls measured slower on GB300 (64^3 collapse: 43.2 s against
+# 39.8 s unbatched; the four chains' registers and the hoisted arguments' longer
+# live ranges cost more than the latency they hide), so the emitter keeps one call
+# per exp/log.  batch_transcendentals stays available behind this switch.
+BATCH_TRANSCENDENTALS = False
 
 
 def batch_transcendentals(dag: Dag, order: list, window: int = BATCH_WINDOW, maxb: int = BATCH_MAX,
@@ -274,7 +279,8 @@ def emit_header(dag: Dag, ir_digest: str) -> str:
 
     # RHS only
     w = _Writer(dag)
-    for it in batch_transcendentals(dag, schedule(dag, rhs_roots)):
+    rhs_order = schedule(dag, rhs_roots)
+    for it in (batch_transcendentals(dag, rhs_order) if BATCH_TRANSCENDENTALS else rhs_order):
         w.item(it)
     out.append("template <class M>")
     out.append("WR_NET_HD void wr_net_rhs(const double* X, const double T, double* f) {")
@@ -286,7 +292,8 @@ def emit_header(dag: Dag, ir_digest: str) -> str:
 
     # fused Jacobian + RHS: schedule J row by row, interleaving outputs as they finish
     w = _Writer(dag)
-    items = batch_transcendentals(dag, schedule(dag, overlap_order(dag, jac_roots + rhs_roots)))
+    fused_order = schedule(dag, overlap_order(dag, jac_roots + rhs_roots))
+    items = batch_transcendentals(dag, fused_order) if BATCH_TRANSCENDENTALS else fused_order
     order = []
     for it in items:
         order.append(it)
