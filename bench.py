@@ -194,6 +194,34 @@ def precision_form(wr, device, math_mode, grid=16, steps=300):
     }
 
 
+def cta32_form(wr, device, grid=32):
+    """The reference's other GPU policy, gridwide-structured-cta32 (one ROS2S
+    controller per 32-cell tile), next to gridwide-independent on a full ``grid``^3
+    collapse: device time of wr_run with the state resident, cell-attempts, and how
+    far the final states differ."""
+    out = {}
+    cells0 = wr.make_grid(grid)
+    res = {}
+    for name, policy in (("independent", wr.POLICY_GRIDWIDE_INDEPENDENT), ("cta32", wr.POLICY_GRIDWIDE_CTA32)):
+        c = cells0.copy()
+        with wr.Context(len(c), device) as ctx:
+            ctx.set_policy(policy)
+            ctx.set_profiling(True)
+            ctx.upload(c)
+            rc, cgs = ctx.run(True)
+            t = ctx.run_timing()
+            ctx.download(c)
+        res[name] = (c, t.run_ms, rc)
+    (ci, ti, _), (ct, tt, rct) = res["independent"], res["cta32"]
+    rT = np.abs(ct["T"] / ci["T"] - 1)
+    out = {"workload": f"{grid}^3 full collapse", "result": int(rct),
+           "cta32_cells_per_s": len(ct) / (tt / 1e3), "independent_cells_per_s": len(ci) / (ti / 1e3),
+           "cta32_over_independent_time": tt / ti,
+           "cell_attempts_ratio": float(ct["stats"]["internal_steps"].sum()) / float(ci["stats"]["internal_steps"].sum()),
+           "T_rel_diff_max": float(rT.max()), "T_rel_diff_median": float(np.median(rT))}
+    return out
+
+
 def cpu_baseline(grid, threads):
     from oracle import oracle
     o = oracle.load("libm")
@@ -294,6 +322,8 @@ def run_gb300(args, rank, ws, local, tdist):
     forms = {}
     if not args.no_forms:
         forms["precision"] = precision_form(wr, local, math_mode)
+        if math_mode == wr.MATH_PORTABLE:
+            forms["cta32_policy"] = cta32_form(wr, local)
     if rank != 0:
         return 0
     cpu = None
@@ -546,7 +576,7 @@ def main():
     ap.add_argument("--cpu-grid", type=int, default=16)
     ap.add_argument("--ref-grid", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-forms", action="store_true", help="skip the precision-form run")
+    ap.add_argument("--no-forms", action="store_true", help="skip the precision-form and cta32-policy runs")
     ap.add_argument("--probe-fp64", action="store_true",
                     help="print this GPU's FP64 issue interval per warp count and the FMA peak, exit")
     ap.add_argument("--diff", action="store_true",

@@ -115,8 +115,12 @@ int wr_grid_dt_history(wr_ctx* ctx, int grid, double* out, int max_steps);
  *    cells (the reference CUDA program, reproducer.cpp:7696-7785).  Default.
  *  WR_POLICY_LEGACY_LOCAL: every cell advances with its own free-fall dt (the
  *    reference CPU program's default, advance_collapse_step, :7646-7685 and the
- *    loop at :8630-8648); its final_states_grid<N>_cpu.bin is reproduced. */
-enum { WR_POLICY_GRIDWIDE_INDEPENDENT = 0, WR_POLICY_LEGACY_LOCAL = 1 };
+ *    loop at :8630-8648); its final_states_grid<N>_cpu.bin is reproduced.
+ *  WR_POLICY_GRIDWIDE_CTA32: the grid-wide dt, and one ROS2S controller per tile of
+ *    32 consecutive cells (tile error = maximum over its cells), the reference's
+ *    structured CUDA policy (advance_collapse_gridwide_structured_kernel,
+ *    structured_cuda.cuh:393-782).  One grid, portable math. */
+enum { WR_POLICY_GRIDWIDE_INDEPENDENT = 0, WR_POLICY_LEGACY_LOCAL = 1, WR_POLICY_GRIDWIDE_CTA32 = 2 };
 int wr_set_policy(wr_ctx* ctx, int policy);
 
 /* Release every device buffer of the context (reproducer.cpp:7967-7973). */

@@ -79,6 +79,8 @@ class Oracle:
         if kind != "ref":
             fn("run_legacy", [vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
                               ctypes.c_int])
+            fn("run_cta32", [vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                             ctypes.c_int])
             for name in ("exp", "log", "cbrt"):
                 fn(name, [ctypes.c_double], ctypes.c_double)
         self.lib = L
@@ -108,6 +110,15 @@ class Oracle:
         cgs = ctypes.c_int(0)
         rc = self._f["run_legacy"](cells.ctypes.data, len(cells), int(bool(perturb)), ctypes.byref(cgs),
                                    int(max_steps), int(nthreads or os.cpu_count() or 1))
+        return rc, cgs.value
+
+    def run_cta32(self, cells, perturb=True, nthreads=None, max_steps=-1):
+        """The gridwide-structured-cta32 policy: one ROS2S controller per 32-cell
+        tile (structured_cuda.cuh:393-782) under the same outer loop."""
+        assert cells.dtype == COLLAPSE_STATE and cells.flags.c_contiguous
+        cgs = ctypes.c_int(0)
+        rc = self._f["run_cta32"](cells.ctypes.data, len(cells), int(bool(perturb)), ctypes.byref(cgs),
+                                  int(max_steps), int(nthreads or os.cpu_count() or 1))
         return rc, cgs.value
 
     def prepare(self, cells, cgs, grid_time, step, perturb=True, nthreads=None):

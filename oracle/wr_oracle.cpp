@@ -19,6 +19,7 @@
 //   (default)             the project's portable exp/log/cbrt (wr_math.h): the
 //                         arithmetic of the GPU library's default mode.
 // Compile with -ffp-contract=off: the reference's rounding sequence has no FMAs.
+#include <algorithm>
 #include <atomic>
 #include <cfloat>
 #include <cmath>
@@ -524,6 +525,185 @@ bool legacy_step(wr_collapse_state& st, int cell, int step, bool perturb, int& f
     return false;
 }
 
+// ---------------------------------------------------------------- gridwide-cta32
+// advance_collapse_gridwide_structured_kernel (structured_cuda.cuh:393-782), for
+// one 32-cell tile: the per-cell prologue (:410-450), then ONE ROS2S controller for
+// the tile (:468-733): a common step h, the tile error = max over participating
+// cells of their error norms (non-finite -> DBL_MAX, :676-688), the Jacobian kept
+// across rejected trials (:496-561), the step-size rules of :689-733, and the
+// commit of :737-768.  Returns the number of cells integrated (0 on failure).
+constexpr int kTile = 32;
+
+double cbrt_nonnegative(double v) {  // structured_cuda.cuh:88-93
+    if (v == 0.0) return 0.0;
+    return OracleMath::exp(OracleMath::log(v) / 3.0);
+}
+
+int advance_tile(wr_collapse_state* cells, int tile_begin, int active, int cgs, double grid_time,
+                 double next_grid_time, double dt_grid, std::atomic<int>& failure) {
+    bool part[kTile] = {false};
+    double base[kTile][NEQ];
+    int count = 0;
+    for (int t = 0; t < active; ++t) {
+        wr_collapse_state& c = cells[tile_begin + t];
+        if (c.completed_steps == cgs) {
+            if (c.time != grid_time) {
+                record_failure(failure, WR_BAD_INPUTS);
+            } else {
+                const double local_dt = collapse_timestep(c);
+                if (local_dt >= 10.0) {
+                    const double old_density = c.density_driver;
+                    c.density_driver += (dt_grid * c.density_driver) / (local_dt / kTffReduc);
+                    if (valid_positive(c.density_driver) && c.density_driver <= 2.0e-6) {
+                        const double ratio = c.density_driver / old_density;
+                        Burn s = load(c);
+                        for (double& x : s.xn) x *= ratio;
+                        s.rho *= ratio;
+                        eos_rt(s);
+                        store(c, s);
+                        part[t] = true;
+                        ++count;
+                    }
+                }
+            }
+        }
+        for (int k = 0; k < NS; ++k) base[t][k] = c.xn[k];
+        base[t][NS] = c.e;
+    }
+    if (count == 0) return 0;
+    const double uround = 1.0e-16, fac_min = 0.2, fac_max = 6.0, safe = 0.9;
+    const int max_steps = 10000000;
+    double h = dt_grid, x = 0.0, hacc = 0.0, erracc = 1.0;
+    bool reject = false, jac_valid = false;
+    int nsing = 0, n_step = 0, n_accept = 0, n_jac = 0, n_rej = 0;
+    int status = WR_SUCCESS;
+    static thread_local double J[kTile][NEQ][NEQ];
+    double f0[kTile][NEQ];
+    while (true) {
+        if (x >= dt_grid || status != WR_SUCCESS) break;
+        if (n_step > max_steps) { status = WR_TOO_MANY_STEPS; continue; }
+        if (0.1 * std::fabs(h) <= std::fabs(x) * uround) { status = WR_DT_UNDERFLOW; continue; }
+        bool final_trial = false;
+        if (x + h * 1.0001 >= dt_grid) {
+            h = dt_grid - x;
+            final_trial = true;
+        }
+        bool singular = false;
+        double err_cell[kTile], cand[kTile][NEQ];
+        for (int t = 0; t < active; ++t) {
+            if (!part[t]) continue;
+            if (!jac_valid) {
+                double Xs[NS], T;
+                state_from_y(base[t], Xs, T);
+                MatSink sink{J[t]};
+                wr_net_jac_rhs<OracleMath>(Xs, T, f0[t], sink);
+            }
+            double e[NEQ][NEQ];
+            int ip[NEQ];
+            for (int i = 0; i < NEQ; ++i) {
+                for (int j = 0; j < NEQ; ++j) e[i][j] = -J[t][i][j];
+                e[i][i] += 1.0 / (h * kGamma);
+            }
+            if (lu_decomposition(e, ip) != 0) { singular = true; continue; }
+            double k1[NEQ], k2[NEQ], w[NEQ], ys[NEQ], dy[NEQ];
+            for (int i = 0; i < NEQ; ++i) k1[i] = f0[t][i];
+            lu_solve(e, ip, k1);
+            for (int i = 0; i < NEQ; ++i) {
+                ys[i] = base[t][i] + kA21 * k1[i];
+                k2[i] = (kC21 / h) * k1[i];
+            }
+            rhs(ys, dy);
+            for (int i = 0; i < NEQ; ++i) k2[i] = dy[i] + k2[i];
+            lu_solve(e, ip, k2);
+            for (int i = 0; i < NEQ; ++i) {
+                ys[i] = base[t][i] + kA31 * k1[i] + kA32 * k2[i];
+                w[i] = (kC31 * k1[i] + kC32 * k2[i]) / h;
+            }
+            rhs(ys, dy);
+            for (int i = 0; i < NEQ; ++i) w[i] = dy[i] + w[i];
+            lu_solve(e, ip, w);
+            double sum = 0.0;
+            for (int i = 0; i < NEQ; ++i) {
+                const double k3 = w[i];
+                cand[t][i] = base[t][i] + kB1 * k1[i] + kB2 * k2[i] + k3;
+                const double est = kE1 * k1[i] + kE2 * k2[i] + kE3 * k3;
+                const double rtol = i == NS ? kRtolEnergy : kRtolSpec;
+                const double atol = i == NS ? kAtolEnergy : kAtolSpec;
+                const double scale = atol + rtol * std::fmax(std::fabs(base[t][i]), std::fabs(cand[t][i]));
+                const double term = est / scale;
+                sum += term * term;
+            }
+            err_cell[t] = std::sqrt(sum / static_cast<double>(NEQ));
+        }
+        if (!jac_valid) n_jac += 1;
+        jac_valid = true;
+        if (singular) {
+            ++nsing;
+            if (nsing >= 5) status = WR_LU_DECOMPOSITION_ERROR;
+            else { h *= 0.5; reject = true; }
+            continue;
+        }
+        double err_tile = 0.0;
+        for (int t = 0; t < active; ++t) {
+            if (!part[t]) continue;
+            double e = err_cell[t];
+            if (!std::isfinite(e)) e = DBL_MAX;
+            err_tile = std::fmax(err_tile, e);
+        }
+        ++n_step;
+        const double fac_step = std::fmax(1.0 / fac_max, std::fmin(1.0 / fac_min, cbrt_nonnegative(err_tile) / safe));
+        double hnew = h / fac_step;
+        if (err_tile <= 1.0) {
+            ++n_accept;
+            if (n_accept > 1) {
+                const double facgus = std::fmax(1.0 / fac_max, std::fmin(1.0 / fac_min,
+                    (hacc / h) * cbrt_nonnegative((err_tile * err_tile) / erracc) / safe));
+                hnew = h / std::fmax(fac_step, facgus);
+            }
+            for (int t = 0; t < active; ++t)
+                if (part[t]) for (int i = 0; i < NEQ; ++i) base[t][i] = cand[t][i];
+            hacc = h;
+            erracc = std::fmax(1.0e-2, err_tile);
+            x = final_trial ? dt_grid : x + h;
+            hnew = std::fmin(std::fabs(hnew), dt_grid);
+            if (reject) hnew = std::fmin(hnew, std::fabs(h));
+            reject = false;
+            h = hnew;
+            jac_valid = false;
+        } else {
+            if (n_accept >= 1) ++n_rej;
+            reject = true;
+            h = hnew;
+        }
+    }
+    if (status != WR_SUCCESS) {
+        record_failure(failure, status);
+        return 0;
+    }
+    for (int t = 0; t < active; ++t) {
+        if (!part[t]) continue;
+        wr_collapse_state& c = cells[tile_begin + t];
+        Burn s = load(c);
+        for (int k = 0; k < NS; ++k) s.xn[k] = base[t][k];
+        s.e = base[t][NS];
+        floor_and_normalize(s);
+        balance_charge(s);
+        floor_and_normalize(s);
+        eos_re(s);
+        store(c, s);
+        c.time = next_grid_time;
+        c.completed_steps = cgs + 1;
+        c.stats.internal_steps += static_cast<uint64_t>(n_step);
+        c.stats.rhs_calls += static_cast<uint64_t>(3 * n_step);
+        c.stats.jacobian_calls += static_cast<uint64_t>(n_jac);
+        c.stats.decompositions += static_cast<uint64_t>(n_step);
+        c.stats.linear_solves += static_cast<uint64_t>(3 * n_step);
+        c.stats.accepted_steps += static_cast<uint64_t>(n_accept);
+        c.stats.rejected_steps += static_cast<uint64_t>(n_rej);
+    }
+    return count;
+}
+
 }  // namespace
 
 extern "C" {
@@ -636,6 +816,37 @@ int wro_run(wr_collapse_state* cells, int n, int perturb, int* cgs, int max_step
         if (!valid_positive(dt_grid) || !std::isfinite(next)) { result = WR_BAD_INPUTS; break; }
         int integrated = 0;
         result = wro_advance(cells, n, *cgs, next, dt_grid, &integrated, nthreads);
+        if (result != WR_SUCCESS) break;
+        if (integrated == 0) break;
+        grid_time = next;
+        *cgs += 1;
+    }
+    return result;
+}
+
+// Host outer loop of the gridwide-structured-cta32 policy (reproducer.cpp:7856-7959
+// with the structured advance launch of :7911-7916): the same prepare and grid
+// minimum, then every 32-cell tile advanced by advance_tile.
+int wro_run_cta32(wr_collapse_state* cells, int n, int perturb, int* cgs, int max_steps, int nthreads) {
+    int result = WR_SUCCESS;
+    double grid_time = 0.0;
+    const int steps = max_steps > 0 ? max_steps : kMaxCollapseSteps;
+    const int tiles = (n + kTile - 1) / kTile;
+    for (int step = 0; result == WR_SUCCESS && step < steps; ++step) {
+        double dt_grid = DBL_MAX;
+        result = wro_prepare(cells, n, *cgs, grid_time, step, perturb, &dt_grid, nthreads);
+        if (result != WR_SUCCESS) break;
+        if (dt_grid == DBL_MAX) break;
+        const double next = grid_time + dt_grid;
+        if (!valid_positive(dt_grid) || !std::isfinite(next)) { result = WR_BAD_INPUTS; break; }
+        std::atomic<int> failure{WR_SUCCESS};
+        int integrated = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : integrated) num_threads(nthreads > 0 ? nthreads : 1)
+        for (int tl = 0; tl < tiles; ++tl) {
+            const int b = tl * kTile;
+            integrated += advance_tile(cells, b, std::min(kTile, n - b), *cgs, grid_time, next, dt_grid, failure);
+        }
+        result = failure.load();
         if (result != WR_SUCCESS) break;
         if (integrated == 0) break;
         grid_time = next;

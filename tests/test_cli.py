@@ -100,3 +100,17 @@ def test_legacy_local_cli_and_manifest(exe, gpu, tmp_path, oracle_port, wr):
     assert "policy=legacy-local-v1" in man and "cell_count=8" in man
     r = run(exe, "--grid", "2", "--write-final-state", str(out), cwd=tmp_path)
     assert r.returncode == 1 and "refusing to overwrite" in r.stderr
+
+
+@pytest.mark.gpu
+def test_cta32_cli(exe, gpu, tmp_path, oracle_port, wr):
+    """--driver-policy gridwide-cta32 prints the reference structured build's policy
+    name and writes the tile-controller final states."""
+    out = tmp_path / "cta32.bin"
+    r = run(exe, "--grid", "2", "--driver-policy", "gridwide-cta32", "--write-final-state", str(out), cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert "driver policy: gridwide-structured-cta32" in r.stdout
+    cells = oracle_port.make_grid(2)
+    oracle_port.run_cta32(cells, perturb=True)
+    assert out.read_bytes() == wr.pack_final_states(cells, 2).tobytes()
+    assert "policy=gridwide-cta32-v1" in (tmp_path / "cta32.bin.manifest").read_text()

@@ -295,3 +295,20 @@ def test_legacy_local_policy_bitwise(wr, gpu, oracle_port, grid):
     rc_o, cgs_o = oracle_port.run_legacy(ref, perturb=True)
     assert rc == rc_o == wr.SUCCESS and cgs == cgs_o
     assert cells.tobytes() == ref.tobytes()
+
+
+@pytest.mark.parametrize("grid", [2, 3, 4, 5])
+def test_cta32_policy_bitwise(wr, gpu, oracle_port, grid):
+    """WR_POLICY_GRIDWIDE_CTA32 (one controller per 32-cell tile, the reference's
+    structured CUDA policy) on the GPU equals the oracle's restatement bit for bit;
+    grid 5 ends in a partial tile (125 = 3 x 32 + 29 cells)."""
+    cells = wr.make_grid(grid)
+    with wr.Context(len(cells)) as ctx:
+        ctx.set_policy(wr.POLICY_GRIDWIDE_CTA32)
+        ctx.upload(cells)
+        rc, cgs = ctx.run(True)
+        ctx.download(cells)
+    ref = oracle_port.make_grid(grid)
+    rc_o, cgs_o = oracle_port.run_cta32(ref, perturb=True)
+    assert rc == rc_o == wr.SUCCESS and cgs == cgs_o
+    assert cells.tobytes() == ref.tobytes()

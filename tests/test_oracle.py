@@ -161,3 +161,24 @@ def test_legacy_local_matches_reference_program(oracle_libm, grid):
     rc, cgs = oracle_libm.run_legacy(cells, perturb=True)
     assert rc == 1
     assert wr.pack_final_states(cells, grid).tobytes() == ref.tobytes()
+
+
+@pytest.mark.parametrize("count", [1, 31, 32, 33])
+def test_cta32_tiles_share_one_controller(oracle_port, count):
+    """gridwide-structured-cta32 restated (structured_cuda.cuh:393-782): the cells
+    of a 32-cell tile take the same substeps (same counters, while every cell of
+    the tile still participates: the first 200 outer steps), partial tiles work,
+    and the result stays near the gridwide-independent one (the tile controller
+    changes trajectories, not the physics)."""
+    a = np.repeat(oracle_port.make_grid(1), count)
+    b = a.copy()
+    rc_i, cgs_i = oracle_port.run(a, perturb=True, nthreads=4, max_steps=200)
+    rc_t, cgs_t = oracle_port.run_cta32(b, perturb=True, nthreads=4, max_steps=200)
+    assert rc_i == rc_t == 1 and cgs_i == cgs_t
+    st = b["stats"]
+    for t in range(0, count, 32):
+        tile = st[t:t + 32]
+        for f in ("internal_steps", "accepted_steps", "rejected_steps", "jacobian_calls"):
+            assert (tile[f] == tile[f][0]).all()
+    assert np.abs(b["T"] / a["T"] - 1).max() < 1e-4
+    assert (b["completed_steps"] == a["completed_steps"]).all()

@@ -38,6 +38,7 @@ MATH_CUDA = 1
 
 POLICY_GRIDWIDE_INDEPENDENT = 0
 POLICY_LEGACY_LOCAL = 1
+POLICY_GRIDWIDE_CTA32 = 2
 
 # CollapseState, reproducer.cpp:7455-7461 (216 bytes)
 STATS_FIELDS = ("internal_steps", "rhs_calls", "jacobian_calls", "decompositions",
@@ -209,7 +210,8 @@ class Context:
             raise WarpReactorError(rc, f"wr_set_advance_variant ({last_error()})")
 
     def set_policy(self, policy: int) -> None:
-        """POLICY_GRIDWIDE_INDEPENDENT (default) or POLICY_LEGACY_LOCAL."""
+        """POLICY_GRIDWIDE_INDEPENDENT (default), POLICY_LEGACY_LOCAL or
+        POLICY_GRIDWIDE_CTA32."""
         rc = lib().wr_set_policy(self.handle, int(policy))
         if rc != SUCCESS:
             raise WarpReactorError(rc, f"wr_set_policy ({last_error()})")

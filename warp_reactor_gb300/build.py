@@ -34,7 +34,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompil
                      "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE, "-I", CSRC]
 CXX_FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fPIC"]
 
-CUDA_UNITS = ["wr_capi.cu", "wr_adv_portable.cu", "wr_adv_cuda.cu", "wr_diag.cu", "wr_noalloc.cu"]
+CUDA_UNITS = ["wr_capi.cu", "wr_adv_portable.cu", "wr_adv_cuda.cu", "wr_adv_cta32.cu", "wr_diag.cu", "wr_noalloc.cu"]
 # differentiation form: relocatable device code, device-linked into one object
 # (its generated derivative code is split over several units that compile in parallel)
 RDC_UNITS = ["wr_diff.cu", "wr_diff_bwd.cu", "wr_diff_net.cu", "wr_diff_jvjp0.cu", "wr_diff_jvjp1.cu"]

@@ -11,9 +11,10 @@
 //   --no-compare-final-state      (default for the GPU backend)
 //   --math portable|cuda          exp/log arithmetic (this program only;
 //                                 default portable, see warp_reactor.h)
-//   --driver-policy gridwide-independent|legacy-local
+//   --driver-policy gridwide-independent|legacy-local|gridwide-cta32
 //                                 outer-step policy (default gridwide-independent;
-//                                 legacy-local is the reference CPU program's)
+//                                 legacy-local is the reference CPU program's,
+//                                 gridwide-cta32 its structured CUDA build's)
 //   --write-final-state FILE      also write the packed final states to FILE with
 //                                 a FILE.manifest sidecar; refuses to overwrite
 //                                 either (the reference's Mojo program's flag,
@@ -165,7 +166,7 @@ void print_usage(const char* program) {
     std::cerr << "usage: " << program
               << " [--grid N] [--perturb|--no-perturb]"
                  " [--compare-final-state FILE|--no-compare-final-state]"
-                 " [--driver-policy gridwide-independent|legacy-local]"
+                 " [--driver-policy gridwide-independent|legacy-local|gridwide-cta32]"
                  " [--write-final-state FILE] [--math portable|cuda]\n";
 }
 
@@ -239,6 +240,8 @@ bool parse_args(int argc, char** argv, Options& o) {  // :8229-8277
                 o.policy = WR_POLICY_GRIDWIDE_INDEPENDENT;
             } else if (p == "legacy-local") {
                 o.policy = WR_POLICY_LEGACY_LOCAL;
+            } else if (p == "gridwide-cta32") {
+                o.policy = WR_POLICY_GRIDWIDE_CTA32;
             } else {
                 print_usage(argv[0]);
                 return false;
@@ -488,11 +491,17 @@ bool compare_from_file(const std::vector<wr_collapse_state>& cells, int grid, co
 // comparison can refuse files from a different program or policy (the Mojo
 // reference writes format, cell count, policy and source hashes,
 // reproducer.mojo:3283-3308).
+const char* policy_name(int policy) {
+    return policy == WR_POLICY_LEGACY_LOCAL ? "legacy-local"
+           : policy == WR_POLICY_GRIDWIDE_CTA32 ? "gridwide-cta32"
+                                                : "gridwide-independent";
+}
+
 std::string manifest_contents(int num_cells, const Options& o) {
     std::ostringstream m;
     m << "format=packed-final-state-v1\n"
       << "cell_count=" << num_cells << "\n"
-      << "policy=" << (o.policy == WR_POLICY_LEGACY_LOCAL ? "legacy-local" : "gridwide-independent") << "-v1\n"
+      << "policy=" << policy_name(o.policy) << "-v1\n"
       << "perturbations=" << (o.perturb ? "enabled" : "disabled") << "\n"
       << "math=" << (o.math == WR_MATH_CUDA ? "cuda" : "portable") << "\n"
       << "program=reproducer_gb300\n";
@@ -589,8 +598,10 @@ int main(int argc, char** argv) {  // reproducer.cpp:8591-8702
     std::cout << "Primordial chemistry collapse grid with ROS2S\n";
     std::cout << "grid: " << o.grid_dim << "^3 (" << num_cells << " cells)\n";
     std::cout << "perturbations: " << (o.perturb ? "enabled" : "disabled") << "\n";
+    // the reference's structured CUDA build prints gridwide-structured-cta32
+    // (reproducer.cpp:8666-8667)
     std::cout << "driver policy: "
-              << (o.policy == WR_POLICY_LEGACY_LOCAL ? "legacy-local" : "gridwide-independent") << "\n";
+              << (o.policy == WR_POLICY_GRIDWIDE_CTA32 ? "gridwide-structured-cta32" : policy_name(o.policy)) << "\n";
     std::cout << "completed global collapse steps: " << cgs << "\n";
     print_collapse_summary(cells);
     std::cout << "wall time: " << elapsed << " s\n";

@@ -69,6 +69,8 @@ struct wr_ctx {
     int graph_policy = -1;
     int policy = WR_POLICY_GRIDWIDE_INDEPENDENT;
     double* local_dt = nullptr;  // legacy-local policy: each cell's own dt
+    double* cta_j = nullptr;     // cta32 policy: per-cell Jacobian [225][n]
+    double* cta_e = nullptr;     // cta32 policy: per-cell iteration matrix [225][n]
     cudaEvent_t ev[4 * WR_MAX_COLLAPSE_STEPS + 2] = {};
     int ev_used = 0;
     wr_run_timing timing{};
@@ -246,6 +248,8 @@ void record(wr_ctx* ctx, int idx) {
 
 cudaError_t launch_advance(wr_ctx* ctx) {
     g_launches.fetch_add(1, std::memory_order_relaxed);
+    if (ctx->policy == WR_POLICY_GRIDWIDE_CTA32)
+        return launch_advance_cta32(cta32_blocks(ctx->n), ctx->stream, ctx->s, ctx->ctl, ctx->cta_j, ctx->cta_e);
     const int blocks = ctx->sms * kAdvanceShapes[ctx->variant].blocks_per_sm;
     if (ctx->math == WR_MATH_CUDA)
         return launch_advance_cuda(ctx->variant, blocks, ctx->stream, ctx->s, ctx->ctl, ctx->jbackup, ctx->ebuf);
@@ -253,6 +257,7 @@ cudaError_t launch_advance(wr_ctx* ctx) {
 }
 
 cudaError_t launch_order(wr_ctx* ctx) {
+    if (ctx->policy == WR_POLICY_GRIDWIDE_CTA32) return cudaSuccess;  // tiles are fixed: no work queue
     g_launches.fetch_add(1, std::memory_order_relaxed);
     k_order<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->s, ctx->ctl);
     return cudaGetLastError();
@@ -412,6 +417,8 @@ void wr_destroy(wr_ctx* ctx) {
     cudaFree(ctx->jbackup);
     cudaFree(ctx->ebuf);
     cudaFree(ctx->local_dt);
+    cudaFree(ctx->cta_j);
+    cudaFree(ctx->cta_e);
     cudaFree(ctx->dt_hist);
     cudaFree(ctx->staging);
     cudaFreeHost(ctx->host_ctl);
@@ -694,14 +701,23 @@ int wr_autotune(wr_ctx* ctx, int perturb, int steps, int* best_variant) {
 
 int wr_set_policy(wr_ctx* ctx, int policy) {
     if (!ctx) return fail_msg("wr_set_policy: null context");
-    if (policy != WR_POLICY_GRIDWIDE_INDEPENDENT && policy != WR_POLICY_LEGACY_LOCAL)
+    if (policy != WR_POLICY_GRIDWIDE_INDEPENDENT && policy != WR_POLICY_LEGACY_LOCAL &&
+        policy != WR_POLICY_GRIDWIDE_CTA32)
         return fail_msg("wr_set_policy: unknown policy");
     if (policy == WR_POLICY_LEGACY_LOCAL && ctx->G != 1) return fail_msg("wr_set_policy: legacy-local needs one grid");
+    if (policy == WR_POLICY_GRIDWIDE_CTA32 && (ctx->G != 1 || ctx->math != WR_MATH_PORTABLE))
+        return fail_msg("wr_set_policy: gridwide-cta32 needs one grid and portable math");
     int rc = set_device(ctx);
     if (rc != WR_SUCCESS) return rc;
     if (policy == WR_POLICY_LEGACY_LOCAL && !ctx->local_dt) {
         const cudaError_t e = cudaMalloc(&ctx->local_dt, static_cast<size_t>(ctx->n) * sizeof(double));
         if (e != cudaSuccess) return fail("cudaMalloc(local dt)", e);
+    }
+    if (policy == WR_POLICY_GRIDWIDE_CTA32 && !ctx->cta_j) {
+        const size_t bytes = static_cast<size_t>(ctx->n) * NEQ * NEQ * sizeof(double);
+        cudaError_t e = cudaMalloc(&ctx->cta_j, bytes);
+        if (e == cudaSuccess) e = cudaMalloc(&ctx->cta_e, bytes);
+        if (e != cudaSuccess) return fail("wr_set_policy cta32 buffers", e);
     }
     ctx->policy = policy;
     ctx->s.local_dt = policy == WR_POLICY_LEGACY_LOCAL ? ctx->local_dt : nullptr;

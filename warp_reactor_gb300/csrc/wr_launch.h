@@ -42,6 +42,11 @@ cudaError_t launch_advance_portable(int variant, int blocks, cudaStream_t stream
 cudaError_t launch_advance_cuda(int variant, int blocks, cudaStream_t stream, DevState s, StepCtl* ctl,
                                 double* jbackup, double* ebuf);
 cudaError_t configure_advance_portable();
+// gridwide-structured-cta32 policy (wr_adv_cta32.cu): one warp per 32-cell tile;
+// jall / eall are per-cell [225][n] Jacobian and iteration-matrix arrays
+cudaError_t launch_advance_cta32(int blocks, cudaStream_t stream, DevState s, StepCtl* ctl, double* jall,
+                                 double* eall);
+int cta32_blocks(int n);
 cudaError_t configure_advance_cuda();
 
 }  // namespace wr
