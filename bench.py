@@ -41,7 +41,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-PUBLISHED_CELLS_PER_S = 15055.0  # H200, the benchmark spec
+PUBLISHED_CELLS_PER_S = 15055.0  # H200, docs/performance/optimization-results.md:51 of the reference
 F_JAC_EXTRA = 104   # burn_state_from_y before each Jacobian (eos_re sums), reproducer.cpp:7029-7038
 F_RHS_EXTRA = 104   # the same before each RHS
 F_LU = 2149         # lu_decomposition<15>: sum_{m=1..14} (1 div + m mul + 2 m^2), reproducer.cpp:96-151
