@@ -491,6 +491,21 @@ def batch_form(args):
     return 0
 
 
+def profile_policy(args):
+    """A fixed run for ncu: one full collapse of the grid with the given policy
+    through wr_run (``--profile-policy independent|cta32``), printing nothing."""
+    import warp_reactor_gb300 as wr
+    from warp_reactor_gb300 import build
+    build.build_all()
+    cells = wr.make_grid(args.grid)
+    policy = wr.POLICY_GRIDWIDE_CTA32 if args.profile_policy == "cta32" else wr.POLICY_GRIDWIDE_INDEPENDENT
+    with wr.Context(len(cells)) as ctx:
+        ctx.set_policy(policy)
+        ctx.upload(cells)
+        rc, _ = ctx.run(True)
+    return 0 if rc == wr.SUCCESS else 1
+
+
 def profile_steps(args):
     """A short, fixed run for ncu: ``--profile-steps S`` outer steps of the grid
     through wr_prepare / wr_advance (the same kernels as wr_run)."""
@@ -535,6 +550,8 @@ def main():
                     help="batching form: 128^3 + 32^3/48^3/80^3/96^3 sub-grids in one context (see --batch-scale)")
     ap.add_argument("--batch-scale", type=float, default=1.0)
     ap.add_argument("--batch-tune-steps", type=int, default=3)
+    ap.add_argument("--profile-policy", choices=("independent", "cta32"), default=None,
+                    help="profiling driver: one full collapse with this policy through wr_run, print nothing, exit")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiling driver: run this many outer steps host-stepped, print nothing, exit")
     args = ap.parse_args()
@@ -544,6 +561,8 @@ def main():
         return diff_form(args)
     if args.batch:
         return batch_form(args)
+    if args.profile_policy:
+        return profile_policy(args)
     if args.profile_steps > 0:
         return profile_steps(args)
     if args.warmup < 3:
