@@ -22,6 +22,13 @@ docs/performance/optimization-results.md:51).
 ``--impl reference`` times the reference's CPU path (the same oracle) instead:
 each step is an 8^3 full collapse on all host cores.
 
+``forms`` in the line: the precision form on a bounded case (16^3, 300 outer
+steps) next to plain FP64, and the gridwide-structured-cta32 policy on the bench
+grid next to the gridwide-independent run.  Other modes: ``--diff`` (the
+differentiation form, 16^3), ``--batch`` (the batching form, 128^3 plus four
+sub-grids), ``--probe-fp64``, and the profiling drivers ``--profile-steps`` and
+``--profile-policy``.
+
 Multi-GPU: the path does not shard (every outer step needs the grid-wide minimum
 over all cells); N > 1 runs N independent replicas, one per GPU.
 """
