@@ -57,6 +57,9 @@ F_ATTEMPT = 541     # stage combinations 375, error norm 96, controller + E = -J
 
 
 def _dist():
+    """Rank, world size, local rank and the process group of a torchrun launch
+    (one replica per GPU).  NCCL on GPUs; gloo where CUDA is absent (CPU tests
+    of the multi-rank path) or when WR_DIST_BACKEND says so."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws <= 1:
         return 0, 1, 0, None
@@ -64,26 +67,40 @@ def _dist():
     import torch.distributed as tdist
     rank = int(os.environ["RANK"])
     local = int(os.environ.get("LOCAL_RANK", rank))
-    torch.cuda.set_device(local)
-    tdist.init_process_group("nccl")
+    backend = os.environ.get("WR_DIST_BACKEND") or ("nccl" if torch.cuda.is_available() else "gloo")
+    if backend == "nccl":
+        torch.cuda.set_device(local)
+    tdist.init_process_group(backend)
     return rank, ws, local, tdist
 
 
+def _on_gpu(tdist):
+    return tdist is not None and tdist.get_backend() == "nccl"
+
+
 def _barrier(tdist):
+    """Barrier with the device drained on both sides (the timed region's edges)."""
     if tdist is not None:
         import torch
-        torch.cuda.synchronize()
+        if _on_gpu(tdist):
+            torch.cuda.synchronize()
         tdist.barrier()
-        torch.cuda.synchronize()
+        if _on_gpu(tdist):
+            torch.cuda.synchronize()
 
 
 def _max_over_ranks(tdist, value):
     if tdist is None:
         return value
     import torch
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    t = torch.tensor([value], dtype=torch.float64, device="cuda" if _on_gpu(tdist) else "cpu")
     tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
     return float(t.item())
+
+
+def whole_job_rate(tdist, world, steps, cells_per_rank, local_seconds):
+    """cells/s of the whole job: every rank's cells over the slowest rank's time."""
+    return world * steps * cells_per_rank / _max_over_ranks(tdist, local_seconds)
 
 
 class ClockSampler:
@@ -304,8 +321,8 @@ def run_gb300(args, rank, ws, local, tdist):
     launches = wr.kernel_launch_count() - launches0
     _barrier(tdist)
     run_s = sum(t.run_ms for t in timings) / 1e3
+    value = whole_job_rate(tdist, ws, args.steps, n, run_s)
     run_s = _max_over_ranks(tdist, run_s)
-    value = ws * args.steps * n / run_s
     ctx.download(out)
     adv_ms = sum(t.advance_ms for t in timings)
     adv_launches = sum(t.advance_launches for t in timings)
