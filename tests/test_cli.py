@@ -85,6 +85,8 @@ def test_policy_and_write_flags_parse(exe):
     for bad in (["--driver-policy"], ["--driver-policy", "cta64"], ["--write-final-state"]):
         r = run(exe, *bad)
         assert r.returncode == 1 and "usage:" in r.stderr, bad
+    r = run(exe, "--help")
+    assert "gridwide-independent|legacy-local|gridwide-cta32" in (r.stdout + r.stderr)
 
 
 @pytest.mark.gpu
