@@ -166,7 +166,11 @@ def algorithmic_ops(cells):
     st = cells["stats"]
     nj = float(st["jacobian_calls"].sum())
     na = float(st["internal_steps"].sum())
-    return nj * f_j + na * f_att, {"F_J": f_j, "F_RHS": f_rhs, "F_attempt": f_att, "jacobians": nj, "attempts": na}
+    # the generated (CSE'd) counts, for reference: the fraction is computed on the
+    # reference's source-level work, so CSE shows as speed, not as lost work
+    cse = {"F_J_plus_RHS_cse": c["cse_jac_rhs_weighted"], "F_RHS_cse": c["cse_rhs_weighted"]}
+    return nj * f_j + na * f_att, {"F_J": f_j, "F_RHS": f_rhs, "F_attempt": f_att, "jacobians": nj, "attempts": na,
+                                   **cse}
 
 
 def precision_form(wr, device, math_mode, grid=16, steps=300):
