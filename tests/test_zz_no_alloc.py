@@ -49,10 +49,9 @@ def test_noalloc_advance_matches_context_advance(wr, gpu):
     dptr = ctypes.c_void_p()
     assert cudart.cudaMalloc(ctypes.byref(dptr), ctypes.c_size_t(nbytes)) == 0  # the caller's own buffer
     try:
-        with wr.Context(len(cells)) as ctx:
+        with wr.Context(len(cells), 0, wr.MATH_PORTABLE) as ctx:
             ctx.upload(cells)
             done, grid_time = 0, 0.0
-            free_after_first = None
             for step in range(2):  # two calls in a row
                 rc, dt = ctx.prepare(done, grid_time, step, True)
                 assert rc == wr.SUCCESS
@@ -71,14 +70,20 @@ def test_noalloc_advance_matches_context_advance(wr, gpu):
                 assert cudart.cudaMemcpy(got.ctypes.data_as(ctypes.c_void_p), dptr, ctypes.c_size_t(nbytes), D2H) == 0
                 assert n.value == n_ctx
                 assert got.tobytes() == want.tobytes()  # bit for bit, like every other parity test
-
-                free_b, total_b = ctypes.c_size_t(), ctypes.c_size_t()
-                assert cudart.cudaMemGetInfo(ctypes.byref(free_b), ctypes.byref(total_b)) == 0
-                if free_after_first is None:
-                    free_after_first = free_b.value
-                else:
-                    assert free_b.value == free_after_first  # the second call allocated nothing
+                last = (pre, done, grid_time + dt, dt)
                 done += 1
                 grid_time += dt
+        # No allocation: free device memory before and after several calls in a
+        # row with nothing else in between (cudaMemGetInfo is device-wide, so an
+        # allocation by any other user of the GPU in between would show as well).
+        free0, free1, total_b = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t()
+        assert cudart.cudaMemGetInfo(ctypes.byref(free0), ctypes.byref(total_b)) == 0
+        pre, cgs, next_time, dt = last
+        for _ in range(3):  # the last step again, from its own input state
+            assert cudart.cudaMemcpy(dptr, pre.ctypes.data_as(ctypes.c_void_p), ctypes.c_size_t(nbytes), H2D) == 0
+            n = ctypes.c_int(-1)
+            assert f(dptr, len(cells), cgs, next_time, dt, ctypes.byref(n)) == wr.SUCCESS
+        assert cudart.cudaMemGetInfo(ctypes.byref(free1), ctypes.byref(total_b)) == 0
+        assert free1.value == free0.value
     finally:
         cudart.cudaFree(dptr)

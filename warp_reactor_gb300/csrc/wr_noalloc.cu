@@ -3,9 +3,9 @@
 //
 // Who needs it: callers that hold their cells in device memory they manage
 // themselves and may not allocate -- a host code running inside another
-// framework's memory pool or allocator, a caller in the middle of building a CUDA
-// graph, a caller on a budgeted or pre-partitioned device -- where the context
-// API's cudaMalloc of state, Jacobian backup and step control is not allowed.
+// framework's memory pool or allocator, or a caller on a budgeted or
+// pre-partitioned device -- where the context API's cudaMalloc of state,
+// Jacobian backup and step control is not allowed.
 //
 // All scratch lives in one file-scope __device__ array of kNoallocScratchBytes
 // (7.9 MiB, held on every GPU that loads the library until the process exits):
@@ -15,10 +15,18 @@
 // re-initialises what must start from zero, and calls that overlap on the GPU
 // (from several host threads or streams) race on it and must not be issued.
 // The first call on a device looks up the array's device address with
-// cudaGetSymbolAddress (with that device current); make that first call before
-// any stream capture.
+// cudaGetSymbolAddress (with that device current) and caches it for the life of
+// the process; do not use the entry point across a cudaDeviceReset of that
+// device.  Every call launches on the legacy default stream and ends with a
+// blocking copy, so no call may be issued while any stream capture is active,
+// and a caller that wrote the cells on a non-blocking stream must order that
+// work before the call (cudaStreamSynchronize or an event).
+//
+// Arithmetic: the portable exp/log/cbrt (WR_MATH_PORTABLE), one lane per cell;
+// the result equals wr_advance of a WR_MATH_PORTABLE context bit for bit.
 #include <cuda_runtime.h>
 
+#include <cstddef>
 #include <mutex>
 #include <string>
 
@@ -35,6 +43,9 @@ constexpr size_t kStateBytes = ((WR_NOALLOC_MAX_CELLS * kStateBytesPerCell + 255
 constexpr size_t kJacBytes = static_cast<size_t>(WR_NOALLOC_LANES) * NEQ * NEQ * sizeof(double);
 constexpr size_t kNoallocScratchBytes = kCtlBytes + kStateBytes + kJacBytes;
 static_assert(sizeof(StepCtl) <= kCtlBytes, "step control must fit its slot");
+// the call reads failure and integrated back with one copy
+static_assert(offsetof(StepCtl, integrated) == offsetof(StepCtl, failure) + sizeof(int),
+              "StepCtl: integrated must follow failure");
 constexpr int kNoallocThreads = 128;  // advance shape 0: 128 lanes per block, matrices in shared memory
 
 // The scratch array.  Host code must not use this name as a device address: it
@@ -139,6 +150,7 @@ extern "C" {
 
 int wr_advance_cells_noalloc(wr_collapse_state* d_cells, int num_cells, int completed_global_steps,
                              double next_grid_time, double dt_grid, int* integrated_out) {
+    g_noalloc_error.clear();
     if (!d_cells || !integrated_out) return noalloc_fail("wr_advance_cells_noalloc: null argument");
     if (num_cells <= 0) return noalloc_fail("wr_advance_cells_noalloc: num_cells must be positive");
     if (num_cells > WR_NOALLOC_MAX_CELLS)
@@ -180,16 +192,18 @@ int wr_advance_cells_noalloc(wr_collapse_state* d_cells, int num_cells, int comp
     double* jbackup = reinterpret_cast<double*>(p + kCtlBytes + kStateBytes);
 
     int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess)
+        return noalloc_fail(std::string("wr_advance_cells_noalloc: device query: ") + cudaGetErrorString(e));
     int blocks = (num_cells + kNoallocThreads - 1) / kNoallocThreads;
     const int max_blocks = WR_NOALLOC_LANES / kNoallocThreads;
     if (blocks > max_blocks) blocks = max_blocks;
-    if (sms > 0 && blocks > sms) blocks = sms;
+    if (blocks > sms) blocks = sms;
 
     const int grid = (num_cells + 255) / 256;
     k_noalloc_unpack<<<grid, 256>>>(d_cells, s, ctl, completed_global_steps, next_grid_time, dt_grid);
-    cudaError_t e = cudaGetLastError();
+    e = cudaGetLastError();
     if (e == cudaSuccess) e = launch_advance_portable(0, blocks, nullptr, s, ctl, jbackup, nullptr);
     if (e == cudaSuccess) {
         k_noalloc_pack<<<grid, 256>>>(s, d_cells);
