@@ -6,8 +6,10 @@
 #  2. on the GPU machine, from the repository root:
 #     sh tests/golden/make_refcuda_fixtures.sh <outdir>
 #     then copy <outdir>/refcuda_grid*.bin into tests/golden/.
+# Without <outdir> the files go to a fresh temporary directory (printed).
 set -e
-OUT=${1:-gpurun_out}
+OUT=${1:-$(mktemp -d)}
+echo "writing to $OUT"
 mkdir -p "$OUT"
 CUDA_HOME=${CUDA_HOME:-/usr/local/cuda}
 g++ -O2 -std=c++17 -I"$CUDA_HOME/include" -o "$OUT/ref_cuda_launcher" oracle/ref_cuda_launcher.cpp \

@@ -137,9 +137,13 @@ WR_MHD double wr_fixed_to_double(int64_t hi, uint64_t lo, int q) {
 
 // Correctly rounded binary64 quotient a/b from integer arithmetic: the result is
 // the IEEE quotient (which is unique), so it can replace a/b anywhere without
-// changing a bit.  Normal operands with a normal quotient take the integer path:
-// a float reciprocal of the divisor's top 24 bits, two fixed-point Newton steps
-// (Q63), a 54-bit quotient, an exact remainder check and round-to-nearest-even.
+// changing a bit.  Method: Newton-Raphson reciprocal iteration followed by an
+// exact remainder correction of the quotient (the Newton-Raphson-based division of
+// J.-M. Muller et al., Handbook of Floating-Point Arithmetic, 2nd ed., Birkhauser
+// 2018), carried out in fixed point.  Normal operands with a normal quotient take
+// the integer path: a float reciprocal of the divisor's top 24 bits, two
+// fixed-point Newton steps (Q63), a 54-bit quotient, an exact remainder check and
+// round-to-nearest-even.
 // Everything else (zeros, subnormals, inf/NaN, overflow/underflow) uses a / b.
 // On GB300 this keeps divisions off the FP64 pipe (a native double division
 // issues about eight FP64 instructions).
