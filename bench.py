@@ -3,30 +3,37 @@
 
 One *step* is one full collapse of the grid: 64^3 = 262,144 cells from the
 reference's initial condition through the 1,000-outer-step free-fall schedule with
-seeded perturbations (the reference's config ``--grid 64``), plain FP64 with the
-library's portable exp/log.  The metric is the reference's: cells / integration
-time (reproducer.cpp:8626-8651; published 15,055 cells/s on H200,
-docs/performance/optimization-results.md:51).
+seeded perturbations (the reference's config ``--grid 64``), plain FP64 with
+CUDA's exp/log -- the arithmetic of the reference's own CUDA build, so the final
+states equal the reference CUDA kernel's bit for bit.  The metric is the
+reference's: cells / integration time (reproducer.cpp:8626-8651; published 15,055
+cells/s on H200, docs/performance/optimization-results.md:51).
 
-  value   device time (CUDA events on the library's stream) of the run with the
-          state already in HBM; L2 is flushed (256 MiB write) before each timed step
+  value   device time of wr_run (the shipped path: CUDA-graph replay of the outer
+          steps), an event pair on the library's stream around the whole run, with
+          the state already in HBM; L2 is flushed (256 MiB write) before each step
   e2e     the same through the public API with host buffers: create, H2D of the
           216-byte records, run, D2H, destroy (wall clock)
   roofline  the advance kernel, FP64-bound: algorithmic FP64 work (the reference's
           source-level operation counts, weighted exp/log = 25, sqrt/cbrt = 20,
           + - * / = 1, times the per-cell Jacobian and attempt counters) over its
-          event-timed duration, against this GPU's measured FP64 FMA rate
+          duration (event nodes inside the graph around every advance launch),
+          against this GPU's measured FP64 FMA rate
+  substeps  ROS2S attempts, accepted, rejected (exact: attempts - accepted) and
+          Jacobians of the timed run, summed over cells
   cpu_baseline  the CPU oracle with C-library math (bitwise the reference's CPU
           arithmetic) on all host cores, on a 16^3 full collapse
 
-``--impl reference`` times the reference's CPU path (the same oracle) instead:
-each step is an 8^3 full collapse on all host cores.
+``forms`` in the line, each after the timed region and within a wall-clock budget
+(``--budget-s``): the reference's own CUDA kernels on the same grid and GPU (their
+time, and whether the final states equal this run's byte for byte), the portable
+exp/log mode with its error against the reference's result, the precision form,
+the gridwide-structured-cta32 policy, the differentiation form (16^3) and the
+batching form (``--forms-batch-scale``).
 
-``forms`` in the line: the precision form on a bounded case (16^3, 300 outer
-steps) next to plain FP64, and the gridwide-structured-cta32 policy on the bench
-grid next to the gridwide-independent run.  Other modes: ``--diff`` (the
-differentiation form, 16^3), ``--batch`` (the batching form, 128^3 plus four
-sub-grids), ``--probe-fp64``, and the profiling drivers ``--profile-steps`` and
+``--impl reference`` times the reference's CPU path (the same CPU oracle) instead:
+each step is a 16^3 full collapse on all host cores.  Other modes: ``--diff``,
+``--batch``, ``--probe-fp64``, and the profiling drivers ``--profile-steps`` and
 ``--profile-policy``.
 
 Multi-GPU: the path does not shard (every outer step needs the grid-wide minimum
@@ -175,7 +182,8 @@ def algorithmic_ops(cells):
 
 def precision_form(wr, device, math_mode, grid=16, steps=300):
     """The precision form (advance variant 3: FP32 factorisation + one FP64 residual
-    refinement per stage solve) next to the plain FP64 form on the first ``steps``
+    refinement per stage solve) next to the plain FP64 form (the default advance) on
+    the first ``steps``
     outer steps of a ``grid``^3 collapse (host-stepped wr_prepare / wr_advance, wall
     clock of synchronous calls): speed, attempts, and the final-state error of the
     precision form against the FP64 result.  A bounded case: the FP32 factorisation
@@ -186,7 +194,8 @@ def precision_form(wr, device, math_mode, grid=16, steps=300):
     def partial(variant):
         c = cells0.copy()
         with wr.Context(len(c), device, math_mode) as ctx:
-            ctx.set_variant(variant)
+            if variant is not None:
+                ctx.set_variant(variant)
             ctx.upload(c)
             t0 = time.perf_counter()
             cgs, gt, rc = 0, 0.0, wr.SUCCESS
@@ -203,7 +212,7 @@ def precision_form(wr, device, math_mode, grid=16, steps=300):
             ctx.download(c)
         return c, el, rc
 
-    ref, t_ref, rc_ref = partial(2)
+    ref, t_ref, rc_ref = partial(None)
     c, t_prec, rc = partial(3)
     rT = np.abs(c["T"] - ref["T"]) / ref["T"]
     big = ref["xn"] > 1e-20
@@ -222,13 +231,13 @@ def precision_form(wr, device, math_mode, grid=16, steps=300):
     }
 
 
-def cta32_form(wr, device, cells0, independent_run_ms, independent_cells):
+def cta32_form(wr, device, math_mode, cells0, independent_run_ms, independent_cells):
     """The reference's other GPU policy, gridwide-structured-cta32 (one ROS2S
     controller per 32-cell tile), on the bench's own grid: device time of wr_run
     with the state resident (L2 flushed), against the gridwide-independent time and
     final state just measured; cell-attempts and how far the final states differ."""
     c = cells0.copy()
-    with wr.Context(len(c), device) as ctx:
+    with wr.Context(len(c), device, math_mode) as ctx:
         ctx.set_policy(wr.POLICY_GRIDWIDE_CTA32)
         ctx.set_profiling(True)
         ctx.upload(c)
@@ -244,6 +253,187 @@ def cta32_form(wr, device, cells0, independent_run_ms, independent_cells):
             "cta32_over_independent_time": t.run_ms / independent_run_ms,
             "cell_attempts_ratio": float(c["stats"]["internal_steps"].sum()) / float(ci["stats"]["internal_steps"].sum()),
             "T_rel_diff_max": float(rT.max()), "T_rel_diff_median": float(np.median(rT))}
+
+
+def substeps(cells):
+    """ROS2S work summed over cells (IntegratorStats, reproducer.cpp:7433-7441):
+    every completed attempt is accepted or rejected, so the exact rejection count
+    is attempts - accepted (rejected_steps itself skips rejections before the
+    first acceptance, :7337)."""
+    st = cells["stats"]
+    att, acc = int(st["internal_steps"].sum()), int(st["accepted_steps"].sum())
+    return {"attempts": att, "accepted": acc, "rejected_exact": att - acc,
+            "rejected_counter": int(st["rejected_steps"].sum()), "jacobians": int(st["jacobian_calls"].sum()),
+            "attempts_per_cell": {"min": int(st["internal_steps"].min()),
+                                  "median": float(np.median(st["internal_steps"])),
+                                  "max": int(st["internal_steps"].max())}}
+
+
+def error_table(wr, cells, ref):
+    """Relative error of ``cells`` against ``ref`` (same grid): T and every species
+    above the 1e-20 abundance floor (max and median), and the substep deltas."""
+    rT = np.abs(cells["T"] - ref["T"]) / np.abs(ref["T"])
+    big = ref["xn"] > 1e-20
+    rx = np.abs(cells["xn"] - ref["xn"])[big] / ref["xn"][big]
+    per = {}
+    for k, name in enumerate(wr.SPECIES):
+        b = big[:, k]
+        if b.any():
+            e = np.abs(cells["xn"][b, k] - ref["xn"][b, k]) / ref["xn"][b, k]
+            per[name] = {"max": float(e.max()), "median": float(np.median(e))}
+    a, r = substeps(cells), substeps(ref)
+    return {"T_rel_err_max": float(rT.max()), "T_rel_err_median": float(np.median(rT)),
+            "species_rel_err_max": float(rx.max()) if rx.size else 0.0,
+            "species_rel_err_median": float(np.median(rx)) if rx.size else 0.0,
+            "per_species": per,
+            "attempts_delta": a["attempts"] - r["attempts"], "accepted_delta": a["accepted"] - r["accepted"],
+            "rejected_delta": a["rejected_exact"] - r["rejected_exact"]}
+
+
+def reference_cuda_form(wr, grid, packed_ours):
+    """The reference's own CUDA kernels (prepare_grid_timestep_kernel and
+    advance_collapse_gridwide_kernel, reproducer.cpp:7696-7785, compiled unmodified
+    for sm_103a) on the same grid and GPU, through the reference's host loop
+    (oracle/ref_cuda_launcher.cpp): wall time, cells/s, substep totals, and whether
+    its final_states file equals this library's final states byte for byte."""
+    import tempfile
+    from warp_reactor_gb300 import build
+    exe = build.ref_cuda_launcher()
+    cubin = os.path.join(ROOT, "oracle", "_ref", "ref_kernels.cubin")
+    if not exe or not os.path.exists(cubin):
+        return {"unavailable": "the reference's CUDA kernels were not built (oracle/_ref/ref_kernels.cubin, "
+                               "made where the reference tree exists)"}
+    with tempfile.TemporaryDirectory() as tmp:
+        out = os.path.join(tmp, f"final_states_grid{grid}_cuda.bin")
+        r = subprocess.run([exe, cubin, str(grid), out], capture_output=True, text=True)
+        if r.returncode != 0:
+            return {"unavailable": f"launcher exited {r.returncode}: {r.stderr.strip()[-200:]}"}
+        line = json.loads(r.stdout.strip().splitlines()[-1])
+        ref = np.fromfile(out, wr.PACKED_FINAL_STATE)
+    line["kind"] = "the reference's CUDA kernels, one thread per cell, 128 per block, its host loop"
+    line["final_states_equal_bytes"] = packed_ours.tobytes() == ref.tobytes()
+    if not line["final_states_equal_bytes"]:
+        rT = np.abs(packed_ours["T"] - ref["T"]) / np.abs(ref["T"])
+        line["T_rel_diff_max"] = float(rT.max())
+    return line
+
+
+def portable_form(wr, device, cells0, ref_cells, headline_run_ms):
+    """The same collapse with the library's portable exp/log/cbrt (integer pipe, no
+    FP64 instructions): its cells/s and its error against the headline run, whose
+    final states are the reference CUDA kernel's."""
+    c = cells0.copy()
+    with wr.Context(len(c), device, wr.MATH_PORTABLE) as ctx:
+        ctx.set_profiling(True)
+        ctx.upload(c)
+        wr.lib().wr_diag_flush_l2(256)
+        rc, cgs = ctx.run(True)
+        t = ctx.run_timing()
+        ctx.download(c)
+    out = {"workload": "the bench grid, full collapse, portable exp/log", "result": int(rc),
+           "cells_per_s": len(c) / (t.run_ms / 1e3), "over_cuda_math_time": t.run_ms / headline_run_ms}
+    out["error_vs_reference"] = error_table(wr, c, ref_cells)
+    return out
+
+
+def diff_measure(grid):
+    """Differentiation form (config 4): 16^3 reference cells, perturbations on, the
+    plain run's schedule; loss = sum over cells of sum_s w_s (log q_s - log t_s)^2
+    over H2, HD, e- and T with a seeded target; gradients in all 15 inputs per cell
+    and the network's log rate multipliers (seeded N(0, 0.1^2)).  Times the forward
+    map and the adjoint (synchronous calls, best of two).  Gradient checks against
+    the FP64 tangent-linear and central differences: tests/test_forms_gpu.py."""
+    import torch
+    import warp_reactor_gb300 as wr
+    from warp_reactor_gb300 import diff
+    cells = wr.make_grid(grid)
+    n = len(cells)
+    t0 = time.perf_counter()
+    sched = diff.schedule(cells)
+    plain_s = time.perf_counter() - t0
+    rng = np.random.default_rng(2024)
+    P = diff.num_multipliers()
+    lm = rng.normal(0.0, 0.1, P)
+    sel = [8, 10, 0, 14]  # H2, HD, e-, T
+    cells_dev = torch.from_numpy(np.ascontiguousarray(cells).view(np.uint8)).cuda()
+    u = torch.from_numpy(diff.initial_u(cells)).cuda()
+    lm_dev = torch.from_numpy(lm).cuda()
+    q = torch.empty((n, 15), dtype=torch.float64, device="cuda")
+    with diff.DiffMap(n) as dm:
+        fwd, bwd = [], []
+        for rep in range(2):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            dm.forward(cells_dev, u, lm_dev, sched, True, q)
+            fwd.append(time.perf_counter() - t)
+            qn = q.cpu().numpy()
+            if rep == 0:
+                target = qn[:, sel] * np.exp(rng.normal(0.0, 0.1, (n, len(sel))))
+            qbar = np.zeros((n, 15))
+            qbar[:, sel] = 2.0 * (np.log(qn[:, sel]) - np.log(target)) / qn[:, sel]
+            ubar = torch.empty((n, 15), dtype=torch.float64, device="cuda")
+            pbar = torch.empty(P, dtype=torch.float64, device="cuda")
+            qbar_dev = torch.from_numpy(qbar).cuda()
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            dm.backward(qbar_dev, ubar, pbar)
+            bwd.append(time.perf_counter() - t)
+        hbuf, counts = dm.record()
+    acc = counts.sum(1)
+    loss = float((((np.log(qn[:, sel]) - np.log(target))) ** 2).sum())
+    return {
+        "form": "differentiation", "grid": grid, "cells": n, "outer_steps": len(sched),
+        "multipliers": P, "loss_species": ["H2", "HD", "e-", "T"], "loss": loss,
+        "forward_s": min(fwd), "adjoint_s": min(bwd), "adjoint_over_forward": min(bwd) / min(fwd),
+        "forward_cells_per_s": n / min(fwd), "plain_run_with_schedule_s": plain_s,
+        "accepted_steps_per_cell": {"min": int(acc.min()), "median": float(np.median(acc)), "max": int(acc.max())},
+        "checkpoints": "outer-step states (18 doubles per cell per step) + burn checkpoints every 32 accepted steps",
+        "grad_norm_u": float(torch.linalg.norm(ubar).item()), "grad_norm_p": float(torch.linalg.norm(pbar).item()),
+        "gradient_checks": "tests/test_forms_gpu.py: adjoint vs the FP64 tangent-linear of the same frozen-controller "
+                           "map (exact), and vs central differences of that map (replayed step sizes)",
+    }
+
+
+def batch_measure(scale, tune_steps, math_mode):
+    """Batching form (config 2): a 128^3 grid plus 32^3, 48^3, 80^3 and 96^3
+    sub-grids of the batching workload (seeded log-normal density sigma = 1 dex,
+    log-uniform T from 100 K to 10^4 K) in one context: one prepare / order /
+    advance launch per outer step covers every cell of every grid, outer steps are
+    replayed from a CUDA graph, the launch shape (lanes per cell among them) is
+    chosen by the autotuner.  ``scale`` multiplies every grid dimension.  Sampled
+    cells of every grid are replayed bit for bit by the oracle in
+    tests/test_forms_gpu.py."""
+    import warp_reactor_gb300 as wr
+    dims = [max(2, int(round(d * scale))) for d in (128, 32, 48, 80, 96)]
+    sizes = [d ** 3 for d in dims]
+    t = time.perf_counter()
+    parts = [wr.make_batch_grid(g, n) for g, n in enumerate(sizes)]
+    gen_s = time.perf_counter() - t
+    cells = np.concatenate(parts)
+    total = len(cells)
+    with wr.Context(grids=sizes, math=math_mode) as ctx:
+        ctx.upload(cells)
+        t = time.perf_counter()
+        best = ctx.autotune(True, steps=tune_steps)
+        tune_s = time.perf_counter() - t
+        ctx.set_profiling(True)
+        wr.lib().wr_diag_flush_l2(256)
+        t = time.perf_counter()
+        rc, cgs = ctx.run(True)
+        run_s = time.perf_counter() - t
+        timing = ctx.run_timing()
+        results = [ctx.grid_result(g) for g in range(len(sizes))]
+        ctx.download(cells)
+    st = cells["stats"]["internal_steps"]
+    return {
+        "form": "batching", "scale": scale, "grids": [f"{d}^3" for d in dims], "cells": total, "result": int(rc),
+        "cells_per_s": total / (timing.run_ms / 1e3), "run_ms": timing.run_ms, "advance_ms": timing.advance_ms,
+        "wall_s": run_s, "autotuned_variant": best, "autotune_s": tune_s, "generate_s": gen_s,
+        "grid_results": [list(r) for r in results],
+        "attempts_per_cell": {"min": int(st.min()), "median": float(np.median(st)), "max": int(st.max()),
+                              "max_over_median": float(st.max() / max(np.median(st), 1))},
+        "oracle_checks": "tests/test_forms_gpu.py (sampled cells of every grid, bit for bit)",
+    }
 
 
 def cpu_baseline(grid, threads):
@@ -291,7 +481,26 @@ def run_reference(args, rank, ws, tdist):
     return 0
 
 
+def _profile_figures():
+    """Figures of the committed ncu capture of the advance kernel (one launch of the
+    64^3 collapse): DRAM bytes per launch and FP64 pipe activity.  Read from
+    profiles/, where the capture's command and summary are kept."""
+    path = os.path.join(ROOT, "profiles", "k_advance_coop_grid64_traffic.txt")
+    out = {}
+    if os.path.exists(path):
+        for ln in open(path):
+            if ":" in ln and not ln.startswith("#"):
+                k, v = ln.split(":", 1)
+                try:
+                    out[k.strip()] = float(v)
+                except ValueError:
+                    pass
+        out["source"] = "profiles/k_advance_coop_grid64_traffic.txt"
+    return out
+
+
 def run_gb300(args, rank, ws, local, tdist):
+    t_start = time.perf_counter()
     import warp_reactor_gb300 as wr
     from warp_reactor_gb300 import build
     build.build_all()
@@ -300,7 +509,7 @@ def run_gb300(args, rank, ws, local, tdist):
     cells0 = wr.make_grid(grid)
     n = len(cells0)
     ctx = wr.Context(n, local, math_mode)
-    ctx.set_profiling(True)
+    ctx.set_profiling(True)  # event nodes in the graph: per-kernel times of the shipped path
     out = np.empty_like(cells0)
 
     def one_step():
@@ -333,6 +542,7 @@ def run_gb300(args, rank, ws, local, tdist):
     ops, opinfo = algorithmic_ops(out)
     peak = wr.fp64_peak()
     achieved = ops * args.steps / (adv_ms / 1e3)
+    step_s = run_s / args.steps
 
     # e2e through the public API with host buffers (timed on the host)
     e2e_cells = cells0.copy()
@@ -343,11 +553,31 @@ def run_gb300(args, rank, ws, local, tdist):
     if rc != wr.SUCCESS:
         raise RuntimeError(f"e2e run failed with {rc}")
     ctx.close()
+
+    # forms: after the timed region, each only if the wall-clock budget allows
     forms = {}
-    if not args.no_forms:
-        forms["precision"] = precision_form(wr, local, math_mode)
-        if math_mode == wr.MATH_PORTABLE:
-            forms["cta32_policy"] = cta32_form(wr, local, cells0, timings[-1].run_ms, out)
+
+    def budget_ok(name, est_s):
+        left = args.budget_s - (time.perf_counter() - t_start)
+        if est_s > left:
+            forms[name] = {"skipped": f"wall-clock budget: needs ~{est_s:.0f} s, {left:.0f} s left of --budget-s"}
+            return False
+        return True
+
+    if not args.no_forms and rank == 0:
+        packed = wr.pack_final_states(out, grid)
+        if math_mode == wr.MATH_CUDA and budget_ok("reference_cuda_kernel", 70.0):
+            forms["reference_cuda_kernel"] = reference_cuda_form(wr, grid, packed)
+        if math_mode == wr.MATH_CUDA and budget_ok("portable_math", 1.5 * step_s + 10):
+            forms["portable_math"] = portable_form(wr, local, cells0, out, timings[-1].run_ms)
+        if budget_ok("cta32_policy", 2.0 * step_s + 10):
+            forms["cta32_policy"] = cta32_form(wr, local, math_mode, cells0, timings[-1].run_ms, out)
+        if budget_ok("differentiation", 60.0):
+            forms["differentiation"] = diff_measure(args.diff_grid)
+        if budget_ok("batching", 150.0 * args.forms_batch_scale ** 3 + 30):
+            forms["batching"] = batch_measure(args.forms_batch_scale, args.batch_tune_steps, math_mode)
+        if budget_ok("precision", 60.0):
+            forms["precision"] = precision_form(wr, local, math_mode)
     if rank != 0:
         return 0
     cpu = None
@@ -357,12 +587,8 @@ def run_gb300(args, rank, ws, local, tdist):
         cpu = {"value": v, "unit": "cells/s", "cores": threads, "kind": "port",
                "sample": f"{args.cpu_grid}^3 full collapse ({args.cpu_grid ** 3} cells, {dt:.1f} s), CPU oracle with "
                          f"C-library math (bitwise the reference CPU build), OpenMP over cells"}
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "k_advance_grid64_traffic.txt")
-    if os.path.exists(tpath):
-        for ln in open(tpath):
-            if ln.startswith("bytes_per_launch:"):
-                traffic = float(ln.split(":", 1)[1])
+    prof = _profile_figures()
+    variant_names = {6: "cooperative advance, 16 lanes per cell (generated vector programs, warp-cooperative LU)"}
     line = {
         "metric": "cells/s, 64^3 collapse", "value": value, "unit": "cells/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * run_s / args.steps, "higher_is_better": True,
@@ -370,12 +596,19 @@ def run_gb300(args, rank, ws, local, tdist):
         "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"{grid}^3 gridwide-independent collapse, 1000 outer steps, perturbations on, "
                                f"plain FP64, {args.math} exp/log", "grid": grid, "cells": n, "outer_steps": cgs,
-                   "form": "plain-fp64 persistent lane-refill advance", "l2": "flushed (256 MiB write) before each step",
-                   "parallelism": f"replicas{ws}"},
+                   "form": variant_names.get(6), "path": "wr_run: CUDA-graph replay of 16 outer steps per launch",
+                   "l2": "flushed (256 MiB write) before each step", "parallelism": f"replicas{ws}"},
+        "substeps": substeps(out),
         "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12,
                      "unit": "T FP64-op/s (weighted, FMA instruction = 1)", "frac": achieved / peak,
-                     "traffic": traffic, "peak_source": "measured live: wr_diag_fp64_peak (DFMA chains, all SMs)",
-                     "kernel": "k_advance", "launches": adv_launches,
+                     "traffic": prof.get("bytes_per_launch"),
+                     "peak_source": "measured live: wr_diag_fp64_peak (DFMA chains, all SMs); MEASURED_PEAKS.json "
+                                    "has no FP64 figure",
+                     "frac_meaning": "algorithm-equivalent: the reference's source-level FP64 work (no CSE, exp/log "
+                                     "weighted 25) per second over the FP64 FMA peak",
+                     "fp64_pipe_active_ncu": prof.get("fp64_pipe_active"),
+                     "profile_source": prof.get("source"),
+                     "kernel": "k_advance_coop", "launches": adv_launches,
                      "ms_per_launch": adv_ms / max(adv_launches, 1), "algorithmic_ops_per_step": ops, **opinfo},
         "cpu_baseline": cpu,
         "e2e": {"value": ws * n / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": n * 216,
@@ -384,6 +617,7 @@ def run_gb300(args, rank, ws, local, tdist):
         "forms": forms,
         "clocks": clocks.summary(),
         "wall_s_timed": t_wall,
+        "wall_s_total": time.perf_counter() - t_start,
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -411,111 +645,20 @@ def probe_fp64():
 
 
 def diff_form(args):
-    """Differentiation form (--diff): 16^3 reference cells, perturbations on, the
-    plain run's schedule; loss = sum over cells of sum_s w_s (log q_s - log t_s)^2
-    over H2, HD, e- and T with a seeded target; gradients in all 15 inputs per
-    cell and the network's log rate multipliers (seeded N(0, 0.1^2)).  Times the
-    forward map and the adjoint (both synchronous calls).  The gradients of this
-    workload are checked against the FP64 tangent-linear and central differences
-    by tests/test_forms_gpu.py."""
-    import torch
-    import warp_reactor_gb300 as wr
-    from warp_reactor_gb300 import build, diff
+    """--diff: the differentiation form alone (see diff_measure)."""
+    from warp_reactor_gb300 import build
     build.build_all()
-    grid = args.diff_grid
-    cells = wr.make_grid(grid)
-    n = len(cells)
-    t0 = time.perf_counter()
-    sched = diff.schedule(cells)
-    plain_s = time.perf_counter() - t0
-    rng = np.random.default_rng(2024)
-    P = diff.num_multipliers()
-    lm = rng.normal(0.0, 0.1, P)
-    sel = [8, 10, 0, 14]  # H2, HD, e-, T
-    cells_dev = torch.from_numpy(np.ascontiguousarray(cells).view(np.uint8)).cuda()
-    u = torch.from_numpy(diff.initial_u(cells)).cuda()
-    lm_dev = torch.from_numpy(lm).cuda()
-    q = torch.empty((n, 15), dtype=torch.float64, device="cuda")
-    with diff.DiffMap(n) as dm:
-        fwd, bwd = [], []
-        for rep in range(2):
-            torch.cuda.synchronize()
-            t = time.perf_counter()
-            dm.forward(cells_dev, u, lm_dev, sched, True, q)
-            fwd.append(time.perf_counter() - t)
-            qn = q.cpu().numpy()
-            if rep == 0:
-                target = qn[:, sel] * np.exp(rng.normal(0.0, 0.1, (n, len(sel))))
-            qbar = np.zeros((n, 15))
-            qbar[:, sel] = 2.0 * (np.log(qn[:, sel]) - np.log(target)) / qn[:, sel]
-            ubar = torch.empty((n, 15), dtype=torch.float64, device="cuda")
-            pbar = torch.empty(P, dtype=torch.float64, device="cuda")
-            qbar_dev = torch.from_numpy(qbar).cuda()
-            torch.cuda.synchronize()
-            t = time.perf_counter()
-            dm.backward(qbar_dev, ubar, pbar)
-            bwd.append(time.perf_counter() - t)
-        hbuf, counts = dm.record()
-    acc = counts.sum(1)
-    loss = float((((np.log(qn[:, sel]) - np.log(target))) ** 2).sum())
-    line = {
-        "form": "differentiation", "grid": grid, "cells": n, "outer_steps": len(sched),
-        "multipliers": P, "loss_species": ["H2", "HD", "e-", "T"], "loss": loss,
-        "forward_s": min(fwd), "adjoint_s": min(bwd), "adjoint_over_forward": min(bwd) / min(fwd),
-        "forward_cells_per_s": n / min(fwd), "plain_run_with_schedule_s": plain_s,
-        "accepted_steps_per_cell": {"min": int(acc.min()), "median": float(np.median(acc)), "max": int(acc.max())},
-        "checkpoints": "outer-step states (18 doubles per cell per step) + burn checkpoints every 32 accepted steps",
-        "grad_norm_u": float(torch.linalg.norm(ubar).item()), "grad_norm_p": float(torch.linalg.norm(pbar).item()),
-        "gradient_checks": "tests/test_forms_gpu.py (tangent-linear and central differences on this workload)",
-    }
-    print(json.dumps(line), flush=True)
+    print(json.dumps(diff_measure(args.diff_grid)), flush=True)
     return 0
 
 
 def batch_form(args):
-    """Batching form (--batch): a 128^3 grid plus 32^3, 48^3, 80^3 and 96^3
-    sub-grids of the batching workload (seeded log-normal density sigma = 1 dex,
-    log-uniform T from 100 K to 10^4 K) in one context: one prepare / order /
-    advance launch per outer step covers every cell of every grid, outer steps are
-    replayed from a CUDA graph, and the launch shape is chosen by the autotuner.
-    --batch-scale s multiplies every grid dimension by s.  Sampled cells of every
-    grid of this workload are replayed bit for bit by the oracle in
-    tests/test_forms_gpu.py."""
+    """--batch: the batching form alone (see batch_measure), full size by default."""
     import warp_reactor_gb300 as wr
     from warp_reactor_gb300 import build
     build.build_all()
-    dims = [max(2, int(round(d * args.batch_scale))) for d in (128, 32, 48, 80, 96)]
-    sizes = [d ** 3 for d in dims]
-    t = time.perf_counter()
-    parts = [wr.make_batch_grid(g, n) for g, n in enumerate(sizes)]
-    gen_s = time.perf_counter() - t
-    cells = np.concatenate(parts)
-    total = len(cells)
-    with wr.Context(grids=sizes) as ctx:
-        ctx.upload(cells)
-        t = time.perf_counter()
-        best = ctx.autotune(True, steps=args.batch_tune_steps)
-        tune_s = time.perf_counter() - t
-        ctx.set_profiling(True)
-        wr.lib().wr_diag_flush_l2(256)
-        t = time.perf_counter()
-        rc, cgs = ctx.run(True)
-        run_s = time.perf_counter() - t
-        timing = ctx.run_timing()
-        results = [ctx.grid_result(g) for g in range(len(sizes))]
-        ctx.download(cells)
-    assert rc == wr.SUCCESS, rc
-    st = cells["stats"]["internal_steps"]
-    line = {
-        "form": "batching", "grids": [f"{d}^3" for d in dims], "cells": total,
-        "cells_per_s": total / (timing.run_ms / 1e3), "run_ms": timing.run_ms, "advance_ms": timing.advance_ms,
-        "wall_s": run_s, "autotuned_variant": best, "autotune_s": tune_s, "generate_s": gen_s,
-        "grid_results": [list(r) for r in results],
-        "attempts_per_cell": {"min": int(st.min()), "median": float(np.median(st)), "max": int(st.max()),
-                              "max_over_median": float(st.max() / max(np.median(st), 1))},
-        "oracle_checks": "tests/test_forms_gpu.py (sampled cells of every grid, bit for bit)",
-    }
-    print(json.dumps(line), flush=True)
+    math_mode = wr.MATH_CUDA if args.math == "cuda" else wr.MATH_PORTABLE
+    print(json.dumps(batch_measure(args.batch_scale, args.batch_tune_steps, math_mode)), flush=True)
     return 0
 
 
@@ -564,11 +707,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     ap.add_argument("--grid", type=int, default=64)
-    ap.add_argument("--math", choices=("portable", "cuda"), default="portable")
+    ap.add_argument("--math", choices=("cuda", "portable"), default="cuda")
     ap.add_argument("--cpu-grid", type=int, default=16)
-    ap.add_argument("--ref-grid", type=int, default=8)
+    ap.add_argument("--ref-grid", type=int, default=16)
+    ap.add_argument("--budget-s", type=float, default=1500.0,
+                    help="wall-clock budget of the whole run: forms that would exceed it are skipped")
+    ap.add_argument("--forms-batch-scale", type=float, default=0.5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-forms", action="store_true", help="skip the precision-form and cta32-policy runs")
+    ap.add_argument("--no-forms", action="store_true", help="skip the forms after the timed region")
     ap.add_argument("--probe-fp64", action="store_true",
                     help="print this GPU's FP64 issue interval per warp count and the FMA peak, exit")
     ap.add_argument("--diff", action="store_true",

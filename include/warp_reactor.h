@@ -83,9 +83,14 @@ typedef struct wr_packed_final_state {
 #pragma pack(pop)
 
 /* Arithmetic used for exp/log/cbrt on the device.
+ *  WR_MATH_CUDA: CUDA's libm, the arithmetic of the reference's own CUDA build
+ *    (reproducer.cpp compiled by nvcc): every result, substep count included,
+ *    equals the reference CUDA kernel's bit for bit.  The default of
+ *    wr_run_cells, the CLI and the Python mirror.
  *  WR_MATH_PORTABLE: the project's own bit-reproducible exp/log/cbrt (integer
- *    fixed-point cores), identical on the GPU and in the CPU oracle.  Default.
- *  WR_MATH_CUDA: CUDA's libm, the arithmetic of the reference's own CUDA build. */
+ *    fixed-point cores, no FP64 instructions), identical on the GPU and in the
+ *    CPU oracle; within an ulp of CUDA's and glibc's, which the adaptive
+ *    controller amplifies to ~1e-5 relative in final T over a collapse. */
 enum { WR_MATH_PORTABLE = 0, WR_MATH_CUDA = 1 };
 
 typedef struct wr_ctx wr_ctx;
@@ -119,7 +124,7 @@ int wr_grid_dt_history(wr_ctx* ctx, int grid, double* out, int max_steps);
  *  WR_POLICY_GRIDWIDE_CTA32: the grid-wide dt, and one ROS2S controller per tile of
  *    32 consecutive cells (tile error = maximum over its cells), the reference's
  *    structured CUDA policy (advance_collapse_gridwide_structured_kernel,
- *    structured_cuda.cuh:393-782).  One grid, portable math. */
+ *    structured_cuda.cuh:393-782).  One grid. */
 enum { WR_POLICY_GRIDWIDE_INDEPENDENT = 0, WR_POLICY_LEGACY_LOCAL = 1, WR_POLICY_GRIDWIDE_CTA32 = 2 };
 int wr_set_policy(wr_ctx* ctx, int policy);
 
@@ -173,41 +178,54 @@ typedef struct wr_run_timing {
 int wr_set_profiling(wr_ctx* ctx, int on);
 
 /* Launch shape of the advance kernel (the knob the autotuner sweeps):
- *   0  128 lanes per SM, per-lane iteration matrix in shared memory
- *   1  256 lanes per SM (2 blocks of 128), iteration matrix in global memory
- *   2  256 lanes per SM (1 block of 256), iteration matrix in global memory
+ *   0  one lane per cell, 128 lanes per SM, iteration matrix in shared memory
+ *   1  one lane per cell, 256 lanes per SM (2 blocks of 128), matrix in global memory
+ *   2  one lane per cell, 256 lanes per SM (1 block of 256), matrix in global memory
  *   3  the precision form: 256 lanes per SM, the iteration matrix factorised in
  *      FP32 with one FP64-residual refinement sweep per stage solve; RHS,
  *      exp/log, stage combination, error norm, controller and EOS stay FP64
- *   4  384 lanes per SM (1 block), iteration matrix in global memory
- * Variants 0-2 and 4 give identical results (only the speed differs); variant 3
- * approximates the FP64 result.  No reference
- * counterpart (the reference fixes 128 threads per block, reproducer.cpp:7398). */
+ *   4  one lane per cell, 384 lanes per SM (1 block), matrix in global memory
+ *   5  cooperative: 8 lanes per cell (4 cells per warp), 6 warps per SM
+ *   6  cooperative: 16 lanes per cell (2 cells per warp), 12 warps per SM (default)
+ *   7  cooperative: 32 lanes per cell (1 cell per warp), 16 warps per SM
+ * The cooperative advance evaluates one cell's network, LU factorisation and
+ * triangular solves with a group of lanes (generated vector programs, a
+ * warp-cooperative LU with shuffle pivot search, shared-memory matrices).
+ * Variants 0-2 and 4-7 give identical results (only the speed differs); variant
+ * 3 approximates the FP64 result.  No reference counterpart (the reference fixes
+ * one thread per cell, 128 threads per block, reproducer.cpp:7398). */
 int wr_set_advance_variant(wr_ctx* ctx, int variant);
 
 /* Autotuner: times the first `steps` outer steps of the uploaded state with each
- * exact launch shape (variants 0-2 and 4), restores the state, selects the fastest and
- * returns it in *best_variant.  The precision form is never chosen by it. */
+ * exact launch shape (variants 0-2 and 4-7: lanes per cell 1, 8, 16, 32 and the
+ * lane-per-cell block shapes), restores the state, selects the fastest and returns
+ * it in *best_variant.  The precision form is never chosen by it. */
 int wr_autotune(wr_ctx* ctx, int perturb, int steps, int* best_variant);
 int wr_get_run_timing(wr_ctx* ctx, wr_run_timing* out);
 
 /* Drop-in for run_cells_cuda (reproducer.cpp:7791-7975): create, upload, run,
- * download, destroy, on the current CUDA device. */
+ * download, destroy, on the current CUDA device, with WR_MATH_CUDA (the
+ * reference CUDA build's arithmetic, so the result is the reference's). */
 int wr_run_cells(wr_collapse_state* cells, int num_cells, int perturb,
                  int* completed_global_steps);
 
 /* No-allocation advance.  Some callers cannot allocate device memory: they keep
  * their cells in device buffers owned by another framework's allocator or pool,
  * or run on a device whose memory is budgeted for them.  This entry point runs
- * one advance step (the same result as wr_advance on those cells) on
- * num_cells <= WR_NOALLOC_MAX_CELLS records in the caller's device memory,
- * updated in place, and allocates nothing: its scratch is one fixed file-scope
- * device array (7.9 MiB, resident on every GPU that loads the library until the
- * process exits).  Calls share that array, so calls that overlap on the GPU race;
+ * one advance step on num_cells <= WR_NOALLOC_MAX_CELLS records in the caller's
+ * device memory, updated in place, and allocates nothing: its scratch is one
+ * fixed file-scope device array (7.9 MiB, resident on every GPU that loads the
+ * library until the process exits).  Its arithmetic is WR_MATH_PORTABLE: the
+ * result equals wr_advance of a WR_MATH_PORTABLE context on those cells bit for
+ * bit.  Calls share the scratch array, so calls that overlap on the GPU race;
  * issue them one at a time.  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress) and must come before any stream capture.
- * It runs on the legacy default stream and returns after the step completes,
- * with *integrated_out = cells committed.  No counterpart in the reference. */
+ * device address (cudaGetSymbolAddress) and caches it for the process; do not
+ * use the entry point across a cudaDeviceReset of that device.  Every call runs
+ * on the legacy default stream and returns after the step completes (a blocking
+ * copy), with *integrated_out = cells committed: issue no call while any stream
+ * capture is active, and order the caller's own writes to the cells on
+ * non-blocking streams before the call (cudaStreamSynchronize or an event).
+ * No counterpart in the reference. */
 #define WR_NOALLOC_MAX_CELLS 4096
 #define WR_NOALLOC_LANES 4096
 int wr_advance_cells_noalloc(wr_collapse_state* d_cells, int num_cells, int completed_global_steps,

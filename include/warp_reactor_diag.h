@@ -32,6 +32,21 @@ int wr_diag_network(int n, const double* X, const double* T, int math_mode,
  * solve runs only where info == 0 (x = b otherwise). */
 int wr_diag_lu(int n, const double* A, const double* b, double* LU, int* ipvt, int* info, double* x);
 
+/* The cooperative advance's generated vector programs (lanes_per_cell = 8, 16 or
+ * 32 lanes evaluating one cell) at n ROS2S states y (n x 15: 14 number densities
+ * and the internal energy): burn_state_from_y (floor, T from e) followed by the
+ * fused Jacobian + RHS program (J: n x 225, f: n x 15) and by the RHS-only program
+ * (f_rhs: n x 15).  The reference evaluates these in jacobian() / rhs() of its
+ * ROS2S system (reproducer.cpp:7029-7049). */
+int wr_diag_coop_network(int lanes_per_cell, int n, const double* y, int math_mode, double* J, double* f,
+                         double* f_rhs);
+
+/* The cooperative (lanes_per_cell = 8, 16 or 32) LU factorisation and triangular
+ * solve of the advance kernel on n 15x15 systems; arguments as wr_diag_lu.
+ * Replaces lu_decomposition<15> / lu_solve<15> (reproducer.cpp:96-181). */
+int wr_diag_coop_lu(int lanes_per_cell, int n, const double* A, const double* b, double* LU, int* ipvt,
+                    int* info, double* x);
+
 /* Elementwise exp (fn = 0), log (fn = 1) or cbrt (fn = 2) of n values on the
  * device with the given math mode: the functions std::exp / std::log / std::cbrt
  * of the reference's network and controller (reproducer.cpp:342-6994, 7309). */

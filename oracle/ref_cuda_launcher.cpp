@@ -5,7 +5,11 @@
 // (reproducer.cpp:7791-7975), and writes the packed final states of the
 // reference's file format (reproducer.cpp:7488-7505, 8357-8378).  The kernels are
 // found in the cubin by name with the driver API; nothing of the reference is
-// modified.  Usage: ref_cuda_launcher <cubin> <grid> <out.bin> [--no-perturb]
+// modified.  Usage: ref_cuda_launcher <cubin> <grid> <out.bin> [--no-perturb] [--structured]
+// --structured: the cubin holds the reference's structured (gridwide-structured-
+// cta32) advance kernel, launched as the reference's host loop does in that build
+// (reproducer.cpp:7843-7852, 7910-7916): one block of 256 threads per 32-cell tile,
+// its shared storage, and a per-cell Jacobian cache.
 #include <cuda.h>
 
 #include <chrono>
@@ -63,11 +67,20 @@ static wr_collapse_state initial_cell() {
 
 int main(int argc, char** argv) {
     if (argc < 4) {
-        std::fprintf(stderr, "usage: %s <cubin> <grid> <out.bin> [--no-perturb]\n", argv[0]);
+        std::fprintf(stderr, "usage: %s <cubin> <grid> <out.bin> [--no-perturb] [--structured]\n", argv[0]);
         return 2;
     }
     const int grid = std::atoi(argv[2]);
-    const bool perturb = !(argc > 4 && std::string(argv[4]) == "--no-perturb");
+    bool perturb = true, structured = false;
+    for (int a = 4; a < argc; ++a) {
+        const std::string opt(argv[a]);
+        if (opt == "--no-perturb") perturb = false;
+        else if (opt == "--structured") structured = true;
+        else {
+            std::fprintf(stderr, "unknown option %s\n", argv[a]);
+            return 2;
+        }
+    }
     int n = grid * grid * grid;
     std::vector<wr_collapse_state> cells(static_cast<size_t>(n), initial_cell());
     CK(cuInit(0));
@@ -88,19 +101,30 @@ int main(int argc, char** argv) {
         CK(cuFuncGetName(&name, f));
         const std::string s(name);
         if (s.find("prepare_grid_timestep_kernel") != std::string::npos) prep = f;
-        if (s.find("advance_collapse_gridwide_kernel") != std::string::npos &&
-            s.find("structured") == std::string::npos) adv = f;
+        if (structured ? s.find("advance_collapse_gridwide_structured_kernel") != std::string::npos
+                       : (s.find("advance_collapse_gridwide_kernel") != std::string::npos &&
+                          s.find("structured") == std::string::npos))
+            adv = f;
     }
     if (!prep || !adv) {
         std::fprintf(stderr, "reference kernels not found in %s\n", argv[1]);
         return 2;
     }
+    unsigned long long shared_bytes = 0;
+    if (structured) {
+        CUdeviceptr sym;
+        size_t sym_size = 0;
+        CK(cuModuleGetGlobal(&sym, &sym_size, mod, "wr_ref_structured_shared_bytes"));
+        CK(cuMemcpyDtoH(&shared_bytes, sym, sizeof shared_bytes));
+        CK(cuFuncSetAttribute(adv, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, static_cast<int>(shared_bytes)));
+    }
     const auto t0 = std::chrono::steady_clock::now();
-    CUdeviceptr dcells, dcand, dcount, dfail;
+    CUdeviceptr dcells, dcand, dcount, dfail, djac = 0;
     CK(cuMemAlloc(&dcells, cells.size() * sizeof(wr_collapse_state)));
     CK(cuMemAlloc(&dcand, cells.size() * sizeof(double)));
     CK(cuMemAlloc(&dcount, sizeof(int)));
     CK(cuMemAlloc(&dfail, sizeof(int)));
+    if (structured) CK(cuMemAlloc(&djac, cells.size() * 225 * sizeof(double)));
     CK(cuMemcpyHtoD(dcells, cells.data(), cells.size() * sizeof(wr_collapse_state)));
     const int success = 1;
     CK(cuMemcpyHtoD(dfail, &success, sizeof(int)));
@@ -125,8 +149,14 @@ int main(int argc, char** argv) {
         if (!(dtg > 0.0) || !(next - next == 0.0)) { result = -1; break; }
         const int zero = 0;
         CK(cuMemcpyHtoD(dcount, &zero, sizeof(int)));
-        void* aa[] = {&dcells, &n, &cgs, &next, &dtg, &dcount, &dfail};
-        CK(cuLaunchKernel(adv, blocks, 1, 1, block, 1, 1, 0, nullptr, aa, nullptr));
+        if (structured) {
+            void* sa[] = {&dcells, &n, &cgs, &grid_time, &next, &dtg, &djac, &dcount, &dfail};
+            const unsigned tiles = static_cast<unsigned>((n + 31) / 32);
+            CK(cuLaunchKernel(adv, tiles, 1, 1, 256, 1, 1, static_cast<unsigned>(shared_bytes), nullptr, sa, nullptr));
+        } else {
+            void* aa[] = {&dcells, &n, &cgs, &next, &dtg, &dcount, &dfail};
+            CK(cuLaunchKernel(adv, blocks, 1, 1, block, 1, 1, 0, nullptr, aa, nullptr));
+        }
         CK(cuCtxSynchronize());
         int cnt = 0;
         CK(cuMemcpyDtoH(&hf, dfail, sizeof(int)));
@@ -138,8 +168,18 @@ int main(int argc, char** argv) {
     }
     CK(cuMemcpyDtoH(cells.data(), dcells, cells.size() * sizeof(wr_collapse_state)));
     const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-    std::printf("{\"grid\": %d, \"cells\": %d, \"result\": %d, \"completed_global_steps\": %d, \"wall_s\": %.6f, \"cells_per_s\": %.3f}\n",
-                grid, n, result, cgs, wall, n / wall);
+    // substep totals over the grid (IntegratorStats, reproducer.cpp:7433-7441)
+    unsigned long long internal = 0, accepted = 0, rejected = 0, jacobians = 0;
+    for (const wr_collapse_state& c : cells) {
+        internal += c.stats.internal_steps;
+        accepted += c.stats.accepted_steps;
+        rejected += c.stats.rejected_steps;
+        jacobians += c.stats.jacobian_calls;
+    }
+    std::printf("{\"grid\": %d, \"cells\": %d, \"result\": %d, \"completed_global_steps\": %d, \"wall_s\": %.6f, "
+                "\"cells_per_s\": %.3f, \"internal_steps\": %llu, \"accepted_steps\": %llu, \"rejected_steps\": %llu, "
+                "\"jacobian_calls\": %llu}\n",
+                grid, n, result, cgs, wall, n / wall, internal, accepted, rejected, jacobians);
     FILE* f = std::fopen(argv[3], "wb");
     if (!f) return 2;
     for (int c = 0; c < n; ++c) {

@@ -78,7 +78,7 @@ def test_batching_workload_replay(wr, gpu, oracle_port):
     sizes = [d ** 3 for d in dims]
     parts = [wr.make_batch_grid(g, n) for g, n in enumerate(sizes)]
     cells = np.concatenate(parts)
-    with wr.Context(grids=sizes) as ctx:
+    with wr.Context(grids=sizes, math=wr.MATH_PORTABLE) as ctx:
         ctx.upload(cells)
         best = ctx.autotune(True, steps=3)
         assert best in (0, 1, 2, 4)

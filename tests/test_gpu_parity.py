@@ -1,9 +1,9 @@
 """GPU parity: the CUDA library through its C ABI against the CPU oracle.
 
-Integer/index results (steps, counters, pivots) must match exactly.  The library's
-default (portable) arithmetic is the oracle's, so floating-point results must match
-bit for bit too; the CUDA-libm mode is compared with the reference's own CUDA
-kernel outputs (fixtures from the reference run on GB300).
+Integer/index results (steps, counters, pivots) must match exactly.  In portable math
+the library's arithmetic is the oracle's, so floating-point results must match bit
+for bit too; the CUDA-libm mode (the default) is compared with the reference's own
+CUDA kernel outputs (fixtures from the reference run on GB300).
 """
 import ctypes
 import os
@@ -93,11 +93,77 @@ def test_lu_fixtures_bitwise(wr, gpu):
         assert o.lu_solve(LUo, ipo, b[i]).tobytes() == x[i].tobytes()
 
 
+def _y_states(n, seed):
+    rng = np.random.default_rng(seed)
+    X = 10.0 ** rng.uniform(-30, 2, size=(n, 14))
+    e = 10.0 ** rng.uniform(9, 12, size=(n, 1))
+    return np.hstack([X, e])
+
+
+def _same(a, b):
+    a, b = np.asarray(a).ravel(), np.asarray(b).ravel()
+    return bool(((a.view(np.uint64) == b.view(np.uint64)) | (np.isnan(a) & np.isnan(b))).all())
+
+
+@pytest.mark.parametrize("lanes", [8, 16, 32])
+def test_coop_network_bitwise(wr, gpu, oracle_port, lanes):
+    """The cooperative advance's vector programs on the GPU (burn_state_from_y +
+    Jacobian + RHS, and burn_state_from_y + RHS) equal the oracle's jacobian(y) /
+    rhs(y) bit for bit, integration states of a grid-2 run included."""
+    ys = _y_states(300, 5)
+    for steps in (150, 300, 450):
+        cells = oracle_port.make_grid(2)
+        oracle_port.run(cells, max_steps=steps)
+        ys = np.vstack([ys, np.hstack([cells["xn"], cells["e"][:, None]])])
+    ys = np.ascontiguousarray(ys)
+    n = len(ys)
+    J = np.zeros((n, 225))
+    f = np.zeros((n, 15))
+    f2 = np.zeros((n, 15))
+    L = wr.lib()
+    L.wr_diag_coop_network.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 3
+    assert L.wr_diag_coop_network(lanes, n, ys.ctypes.data, wr.MATH_PORTABLE, J.ctypes.data, f.ctypes.data,
+                                  f2.ctypes.data) == 1
+    for i in range(n):
+        assert _same(J[i], oracle_port.jac(ys[i])), i
+        fo = oracle_port.rhs(ys[i])
+        assert _same(f[i], fo) and _same(f2[i], fo), i
+
+
+@pytest.mark.parametrize("lanes", [8, 16, 32])
+def test_coop_lu_fixtures_bitwise(wr, gpu, oracle_port, lanes):
+    """The warp-cooperative LU and solves on the reference's LU fixtures
+    (tests/gpu/test_warp_lu.mojo:19-47 of the reference) and 61 random systems."""
+    g = np.load(os.path.join(GOLDEN, "lu_ref.npz"))
+    rng = np.random.default_rng(7)
+    extra = rng.normal(size=(61, 15, 15)) + 3 * np.eye(15)
+    A = np.ascontiguousarray(np.concatenate([g["A"], extra]))
+    b = np.ascontiguousarray(np.concatenate([g["b"], rng.normal(size=(61, 15))]))
+    n = len(A)
+    LU = np.zeros_like(A)
+    ip = np.zeros((n, 15), np.int32)
+    info = np.zeros(n, np.int32)
+    x = np.zeros_like(b)
+    L = wr.lib()
+    L.wr_diag_coop_lu.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 6
+    assert L.wr_diag_coop_lu(lanes, n, A.ctypes.data, b.ctypes.data, LU.ctypes.data, ip.ctypes.data,
+                             info.ctypes.data, x.ctypes.data) == 1
+    assert (info[:8] == g["info"]).all()
+    assert LU[:8].tobytes() == g["LU"].tobytes()
+    assert (ip[:8] == g["ipvt"]).all()
+    ok = g["info"] == 0
+    assert x[:8][ok].tobytes() == g["x"][ok].tobytes()
+    for i in range(8, n):
+        inf, LUo, ipo = oracle_port.lu(A[i])
+        assert inf == info[i] and LUo.tobytes() == LU[i].tobytes() and (ipo == ip[i]).all()
+        assert oracle_port.lu_solve(LUo, ipo, b[i]).tobytes() == x[i].tobytes()
+
+
 @pytest.mark.parametrize("grid,perturb", [(1, True), (2, True), (3, True), (4, True), (5, True), (2, False),
                                           (8, True)])
 def test_grid_runs_bitwise(wr, gpu, oracle_port, grid, perturb):
     cells = wr.make_grid(grid)
-    rc, cgs = wr.run_cells(cells, perturb)
+    rc, cgs = wr.run_cells(cells, perturb, math=wr.MATH_PORTABLE)
     ref = oracle_port.make_grid(grid)
     rc_o, cgs_o = oracle_port.run(ref, perturb=perturb)
     assert rc == rc_o == wr.SUCCESS
@@ -133,14 +199,21 @@ def test_host_stepped_api_equals_device_loop(wr, gpu):
     assert a.tobytes() == b.tobytes()
 
 
-@pytest.mark.parametrize("grid", [4, 8])
-def test_cuda_math_equals_reference_cuda_kernel(wr, gpu, grid):
+@pytest.mark.parametrize("grid,variant", [(4, None), (8, None), (4, 2), (4, 5), (4, 7)])
+def test_cuda_math_equals_reference_cuda_kernel(wr, gpu, grid, variant):
     """WR_MATH_CUDA reproduces the reference's own CUDA kernels (reproducer.cpp
-    compiled with nvcc --fmad=false for sm_103a and run on GB300) bit for bit."""
+    compiled with nvcc --fmad=false for sm_103a and run on GB300) bit for bit:
+    the default (cooperative, 16 lanes per cell) advance, the lane-per-cell
+    advance (variant 2) and the cooperative advance with 8 and 32 lanes."""
     path = os.path.join(GOLDEN, f"refcuda_grid{grid}.bin")
     ref = np.fromfile(path, wr.PACKED_FINAL_STATE)
     cells = wr.make_grid(grid)
-    rc, cgs = wr.run_cells(cells, True, math=wr.MATH_CUDA)
+    with wr.Context(len(cells), 0, wr.MATH_CUDA) as ctx:
+        if variant is not None:
+            ctx.set_variant(variant)
+        ctx.upload(cells)
+        rc, cgs = ctx.run(True)
+        ctx.download(cells)
     assert rc == wr.SUCCESS
     assert wr.pack_final_states(cells, grid).tobytes() == ref.tobytes()
 
@@ -173,7 +246,7 @@ def test_full_grid_64_replay_sample(wr, gpu, oracle_port):
     the cells that set the grid dt."""
     grid = 64
     cells = wr.make_grid(grid)
-    with wr.Context(len(cells)) as ctx:
+    with wr.Context(len(cells), 0, wr.MATH_PORTABLE) as ctx:
         ctx.upload(cells)
         rc, cgs = ctx.run(True)
         hist = np.zeros(wr.MAX_COLLAPSE_STEPS)
@@ -198,7 +271,7 @@ def test_full_grid_64_replay_sample(wr, gpu, oracle_port):
     assert (cells["time"][live] == cells["time"][live][0]).all()
 
 
-@pytest.mark.parametrize("variant", [1, 2, 4])
+@pytest.mark.parametrize("variant", [0, 1, 2, 4, 5, 7])
 def test_advance_variants_identical(wr, gpu, variant):
     """Every launch shape of the advance kernel gives the same bits."""
     a = wr.make_grid(3)
@@ -222,7 +295,7 @@ def test_precision_form_against_fp64_oracle(wr, gpu, oracle_port):
     cells = wr.make_grid(2)
     ref = oracle_port.make_grid(2)
     gt, gt_o, cgs = 0.0, 0.0, 0
-    with wr.Context(len(cells)) as ctx:
+    with wr.Context(len(cells), 0, wr.MATH_PORTABLE) as ctx:
         ctx.set_variant(3)
         ctx.upload(cells)
         for step in range(20):
@@ -251,7 +324,7 @@ def test_batched_grids_equal_separate_runs(wr, gpu, oracle_port):
     sizes = [8, 27, 64, 125]
     parts = [wr.make_grid(2), wr.make_grid(3), wr.make_grid(4), wr.make_batch_grid(3, 125)]
     cells = np.concatenate(parts)
-    with wr.Context(grids=sizes) as ctx:
+    with wr.Context(grids=sizes, math=wr.MATH_PORTABLE) as ctx:
         ctx.upload(cells)
         rc, _ = ctx.run(True)
         results = [ctx.grid_result(g) for g in range(len(sizes))]
@@ -275,7 +348,7 @@ def test_autotuner_keeps_results(wr, gpu):
     with wr.Context(len(b)) as ctx:
         ctx.upload(b)
         best = ctx.autotune(True, steps=3)
-        assert best in (0, 1, 2, 4)
+        assert best in (0, 1, 2, 4, 5, 6, 7)
         rc, cgs = ctx.run(True)
         ctx.download(b)
     assert rc == wr.SUCCESS and a.tobytes() == b.tobytes()
@@ -286,7 +359,7 @@ def test_legacy_local_policy_bitwise(wr, gpu, oracle_port, grid):
     """WR_POLICY_LEGACY_LOCAL on the GPU equals the oracle's legacy-local loop (the
     reference CPU program's default policy) bit for bit."""
     cells = wr.make_grid(grid)
-    with wr.Context(len(cells)) as ctx:
+    with wr.Context(len(cells), 0, wr.MATH_PORTABLE) as ctx:
         ctx.set_policy(wr.POLICY_LEGACY_LOCAL)
         ctx.upload(cells)
         rc, cgs = ctx.run(True)
@@ -303,7 +376,7 @@ def test_cta32_policy_bitwise(wr, gpu, oracle_port, grid):
     structured CUDA policy) on the GPU equals the oracle's restatement bit for bit;
     grid 5 ends in a partial tile (125 = 3 x 32 + 29 cells)."""
     cells = wr.make_grid(grid)
-    with wr.Context(len(cells)) as ctx:
+    with wr.Context(len(cells), 0, wr.MATH_PORTABLE) as ctx:
         ctx.set_policy(wr.POLICY_GRIDWIDE_CTA32)
         ctx.upload(cells)
         rc, cgs = ctx.run(True)

@@ -145,7 +145,7 @@ class Context:
     covers all of them.
     """
 
-    def __init__(self, num_cells: int = 0, device: int = 0, math: int = MATH_PORTABLE, grids=None):
+    def __init__(self, num_cells: int = 0, device: int = 0, math: int = MATH_CUDA, grids=None):
         h = ctypes.c_void_p()
         if grids is None:
             grids = [int(num_cells)]
@@ -256,7 +256,7 @@ class Context:
         return rc, cgs.value
 
 
-def run_cells(cells: np.ndarray, perturb: bool = True, math: int = MATH_PORTABLE, device: int = 0):
+def run_cells(cells: np.ndarray, perturb: bool = True, math: int = MATH_CUDA, device: int = 0):
     """Mirror of ``run_cells_cuda(cells, perturb, completed_global_steps)``: advances
     ``cells`` in place and returns (IntegratorResult, completed_global_steps)."""
     with Context(len(cells), device, math) as ctx:

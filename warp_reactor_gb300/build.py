@@ -34,7 +34,8 @@ NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompil
                      "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE, "-I", CSRC]
 CXX_FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fPIC"]
 
-CUDA_UNITS = ["wr_capi.cu", "wr_adv_portable.cu", "wr_adv_cuda.cu", "wr_adv_cta32.cu", "wr_diag.cu", "wr_noalloc.cu"]
+CUDA_UNITS = ["wr_capi.cu", "wr_adv_portable.cu", "wr_adv_cuda.cu", "wr_adv_cta32.cu", "wr_diag.cu", "wr_noalloc.cu",
+              "wr_adv_coop8.cu", "wr_adv_coop16.cu", "wr_adv_coop32.cu"]
 # differentiation form: relocatable device code, device-linked into one object
 # (its generated derivative code is split over several units that compile in parallel)
 RDC_UNITS = ["wr_diff.cu", "wr_diff_bwd.cu", "wr_diff_net.cu", "wr_diff_jvjp0.cu", "wr_diff_jvjp1.cu"]
@@ -138,13 +139,34 @@ def build_oracle(verbose=False) -> list:
         tasks.append(["g++"] + CXX_FLAGS + ["-fopenmp", "-shared", "-o", dso, dsrc])
     with cf.ThreadPoolExecutor(max_workers=3) as ex:
         list(ex.map(lambda c: _run(c, verbose), tasks))
+    ref_cuda_launcher(verbose)
     return outs
+
+
+def ref_cuda_launcher(verbose=False) -> str:
+    """Compile the host launcher of the reference's own CUDA kernels (test and
+    benchmark infrastructure: it runs oracle/_ref/ref_kernels.cubin through the
+    reference's host loop).  Returns its path, or "" where the CUDA driver library
+    stub is missing."""
+    src = os.path.join(ORACLE, "ref_cuda_launcher.cpp")
+    exe = os.path.join(ORACLE_OUT, "ref_cuda_launcher")
+    home = _cuda_home()
+    stubs = [d for d in (os.path.join(home, "lib64", "stubs"), os.path.join(home, "targets", "sbsa-linux", "lib", "stubs"),
+                         os.path.join(home, "targets", "x86_64-linux", "lib", "stubs")) if os.path.isdir(d)]
+    if not os.path.exists(src) or not stubs:
+        return ""
+    os.makedirs(ORACLE_OUT, exist_ok=True)
+    if _stale(exe, [src, os.path.join(INCLUDE, "warp_reactor.h")]):
+        _run(["g++", "-O2", "-std=c++17", "-I", os.path.join(home, "include"), "-o", exe, src] +
+             [f"-L{d}" for d in stubs] + ["-lcuda"], verbose)
+    return exe
 
 
 def build_reference_oracle(verbose=False) -> None:
     """Compile the reference itself into oracle/_ref (only where its tree exists)."""
     script = os.path.join(ORACLE, "build_ref.sh")
-    ref_dir = os.environ.get("REF_DIR", "/root/reference")
+    # REF_DIR names the reference checkout; by default its sibling of this repository
+    ref_dir = os.environ.get("REF_DIR") or os.path.join(os.path.dirname(ROOT), "reference")
     ref_src = os.path.join(ref_dir, "reproducer.cpp")
     if not (os.path.exists(ref_src) and os.path.exists(script)):
         return

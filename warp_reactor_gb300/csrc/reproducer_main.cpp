@@ -9,8 +9,9 @@
 //   --compare-final-state FILE    compare with a final_states_grid<N> file
 //   --compare-final-state=FILE
 //   --no-compare-final-state      (default for the GPU backend)
-//   --math portable|cuda          exp/log arithmetic (this program only;
-//                                 default portable, see warp_reactor.h)
+//   --math cuda|portable          exp/log arithmetic (this program only;
+//                                 default cuda: CUDA's libm, the arithmetic of
+//                                 the reference's CUDA build; see warp_reactor.h)
 //   --driver-policy gridwide-independent|legacy-local|gridwide-cta32
 //                                 outer-step policy (default gridwide-independent;
 //                                 legacy-local is the reference CPU program's,
@@ -66,7 +67,7 @@ struct Options {
     int grid_dim = kDefaultGrid;
     bool perturb = true;
     bool show_help = false;
-    int math = WR_MATH_PORTABLE;
+    int math = WR_MATH_CUDA;
     int policy = WR_POLICY_GRIDWIDE_INDEPENDENT;
     std::string write_path;
     std::string compare_path;  // the GPU backend compares only on request (:7467-7468)

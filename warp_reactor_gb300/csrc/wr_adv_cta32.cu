@@ -252,9 +252,12 @@ __global__ void __launch_bounds__(kCtaThreads, 1) k_advance_cta32(DevState s, St
 
 }  // namespace
 
-cudaError_t launch_advance_cta32(int blocks, cudaStream_t stream, DevState s, StepCtl* ctl, double* jall,
-                                 double* eall) {
-    k_advance_cta32<PortableMathCall><<<blocks, kCtaThreads, 0, stream>>>(s, ctl, jall, eall);
+cudaError_t launch_advance_cta32(int math_cuda, int blocks, cudaStream_t stream, DevState s, StepCtl* ctl,
+                                 double* jall, double* eall) {
+    if (math_cuda)
+        k_advance_cta32<CudaMath><<<blocks, kCtaThreads, 0, stream>>>(s, ctl, jall, eall);
+    else
+        k_advance_cta32<PortableMathCall><<<blocks, kCtaThreads, 0, stream>>>(s, ctl, jall, eall);
     return cudaGetLastError();
 }
 

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "../../include/warp_reactor.h"
+#include "wr_coop.cuh"
 #include "wr_launch.h"
 
 using namespace wr;
@@ -50,7 +51,7 @@ struct wr_ctx {
     int math = WR_MATH_PORTABLE;
     int advance_blocks = 0;
     int sms = 1;
-    int variant = 2;  // fastest measured shape (256 lanes per SM, matrices in global memory)
+    int variant = kDefaultVariant;  // the cooperative advance, 16 lanes per cell
     cudaStream_t stream = nullptr;
     DevState s{};
     void* state_buf = nullptr;
@@ -67,6 +68,7 @@ struct wr_ctx {
     cudaGraphExec_t graph = nullptr;
     int graph_variant = -1;
     int graph_policy = -1;
+    int graph_timed = -1;  // the captured graph records the per-kernel events
     int policy = WR_POLICY_GRIDWIDE_INDEPENDENT;
     double* local_dt = nullptr;  // legacy-local policy: each cell's own dt
     double* cta_j = nullptr;     // cta32 policy: per-cell Jacobian [225][n]
@@ -130,6 +132,88 @@ __global__ void k_order(DevState s, StepCtl* ctl) {
     if (b < 0) return;
     const unsigned int pos = atomicAdd(&ctl->off[b], 1u);
     if (pos < static_cast<unsigned int>(s.n)) s.order[pos] = cell;
+}
+
+// Prologue of advance_collapse_gridwide_kernel (reproducer.cpp:7748-7768) for every
+// queued cell, fused with the queue scatter: the cell's free-fall dt check, the
+// driver (density) update with the grid dt, the density limit, the scaling of the
+// number densities and e from T (burn_ros2s prologue, :7594-7606).  The cell is
+// then marked kQBurn (the advance burns it) or kQSkip.  Legacy-local cells were
+// scaled by k_prepare_legacy already.
+__global__ void __launch_bounds__(256) k_order_preburn(DevState s, StepCtl* ctl) {
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= s.n || ctl->all_stop) return;
+    const int b = s.qbucket[cell];
+    if (b < 0) return;
+    const unsigned int pos = atomicAdd(&ctl->off[b], 1u);
+    if (pos < static_cast<unsigned int>(s.n)) s.order[pos] = cell;
+    const int g = s.grid_of ? s.grid_of[cell] : 0;
+    const StepCtl* c = ctl + g;
+    int flag = kQSkip;
+    if (!c->stop && c->failure == WR_SUCCESS && s.steps[cell] == c->cgs) {
+        s.cost[cell] = 0;
+        if (s.local_dt != nullptr) {
+            flag = kQBurn;
+        } else {
+            const int n = s.n;
+            double xn[NS];
+#pragma unroll
+            for (int k = 0; k < NS; ++k) xn[k] = s.xn[k * n + cell];
+            const double local_dt = collapse_timestep(xn);
+            if (!(local_dt < 10.0)) {
+                const double old_density = s.driver[cell];
+                const double tff = ddiv(local_dt, kTffReduc);
+                const double driver = old_density + c->dt_grid * ddiv(old_density, tff);
+                s.driver[cell] = driver;
+                if (valid_positive(driver) && !(driver > kDriverLimit)) {
+                    const double ratio = ddiv(driver, old_density);
+#pragma unroll
+                    for (int k = 0; k < NS; ++k) xn[k] *= ratio;
+                    s.rho[cell] = s.rho[cell] * ratio;
+                    s.e[cell] = eos_e_from_T(xn, s.T[cell]);
+#pragma unroll
+                    for (int k = 0; k < NS; ++k) s.xn[k * n + cell] = xn[k];
+                    flag = kQBurn;
+                }
+            }
+        }
+    }
+    s.qbucket[cell] = flag;
+}
+
+// Commit of a successful burn (advance kernel epilogue, reproducer.cpp:7774-7784):
+// renormalise the number densities, T from e, the grid clock and the step count;
+// the integrated count per sub-grid.
+__global__ void __launch_bounds__(256) k_commit(DevState s, StepCtl* ctl) {
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    bool done = false;
+    int g = 0;
+    if (cell < s.n && !ctl->all_stop && s.qbucket[cell] == kQBurnOK) {
+        const int n = s.n;
+        g = s.grid_of ? s.grid_of[cell] : 0;
+        const StepCtl* c = ctl + g;
+        double xn[NS];
+#pragma unroll
+        for (int k = 0; k < NS; ++k) xn[k] = s.xn[k * n + cell];
+        renormalize(xn, s.rho[cell]);
+        s.T[cell] = eos_T_from_e(xn, s.e[cell]);
+#pragma unroll
+        for (int k = 0; k < NS; ++k) s.xn[k * n + cell] = xn[k];
+        const double dt = s.local_dt ? s.local_dt[cell] : 0.0;
+        s.time[cell] = s.local_dt ? s.time[cell] + dt : c->next_grid_time;
+        s.steps[cell] = c->cgs + 1;
+        s.qbucket[cell] = kQSkip;
+        done = true;
+    }
+    // one atomic per warp when the warp's cells share a sub-grid
+    const unsigned m = __ballot_sync(0xffffffffu, done);
+    const int g0 = __shfl_sync(0xffffffffu, g, __ffs(m ? m : 1u) - 1);
+    const bool uniform = __all_sync(0xffffffffu, !done || g == g0);
+    if (uniform) {
+        if ((threadIdx.x & 31) == 0 && m) atomicAdd(&ctl[g0].integrated, __popc(m));
+    } else if (done) {
+        atomicAdd(&ctl[g].integrated, 1);
+    }
 }
 
 // start of an outer step driven by the host (wr_prepare; one grid)
@@ -246,11 +330,25 @@ void record(wr_ctx* ctx, int idx) {
     if (ctx->profiling) cudaEventRecord(ctx->ev[idx], ctx->stream);
 }
 
+// the cooperative advance runs between k_order_preburn and k_commit
+bool coop_active(const wr_ctx* ctx) {
+    return ctx->policy != WR_POLICY_GRIDWIDE_CTA32 && is_coop(ctx->variant);
+}
+
 cudaError_t launch_advance(wr_ctx* ctx) {
     g_launches.fetch_add(1, std::memory_order_relaxed);
     if (ctx->policy == WR_POLICY_GRIDWIDE_CTA32)
-        return launch_advance_cta32(cta32_blocks(ctx->n), ctx->stream, ctx->s, ctx->ctl, ctx->cta_j, ctx->cta_e);
+        return launch_advance_cta32(ctx->math == WR_MATH_CUDA ? 1 : 0, cta32_blocks(ctx->n), ctx->stream, ctx->s,
+                                    ctx->ctl, ctx->cta_j, ctx->cta_e);
     const int blocks = ctx->sms * kAdvanceShapes[ctx->variant].blocks_per_sm;
+    if (is_coop(ctx->variant)) {
+        const int math_cuda = ctx->math == WR_MATH_CUDA ? 1 : 0;
+        switch (kAdvanceShapes[ctx->variant].coop_lanes) {
+            case 8: return launch_advance_coop8(math_cuda, blocks, ctx->stream, ctx->s, ctx->ctl);
+            case 32: return launch_advance_coop32(math_cuda, blocks, ctx->stream, ctx->s, ctx->ctl);
+            default: return launch_advance_coop16(math_cuda, blocks, ctx->stream, ctx->s, ctx->ctl);
+        }
+    }
     if (ctx->math == WR_MATH_CUDA)
         return launch_advance_cuda(ctx->variant, blocks, ctx->stream, ctx->s, ctx->ctl, ctx->jbackup, ctx->ebuf);
     return launch_advance_portable(ctx->variant, blocks, ctx->stream, ctx->s, ctx->ctl, ctx->jbackup, ctx->ebuf);
@@ -259,7 +357,18 @@ cudaError_t launch_advance(wr_ctx* ctx) {
 cudaError_t launch_order(wr_ctx* ctx) {
     if (ctx->policy == WR_POLICY_GRIDWIDE_CTA32) return cudaSuccess;  // tiles are fixed: no work queue
     g_launches.fetch_add(1, std::memory_order_relaxed);
-    k_order<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->s, ctx->ctl);
+    if (coop_active(ctx))
+        k_order_preburn<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->s, ctx->ctl);
+    else
+        k_order<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->s, ctx->ctl);
+    return cudaGetLastError();
+}
+
+// after the cooperative advance: commit the cells it burned
+cudaError_t launch_commit(wr_ctx* ctx) {
+    if (!coop_active(ctx)) return cudaSuccess;
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    k_commit<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->s, ctx->ctl);
     return cudaGetLastError();
 }
 
@@ -371,6 +480,9 @@ int wr_create_batch(int num_grids, const int* cells_per_grid, int device, int ma
     if (e == cudaSuccess) e = cudaMalloc(&ctx->dt_hist, static_cast<size_t>(ctx->G) * WR_MAX_COLLAPSE_STEPS * sizeof(double));
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->host_ctl, sizeof(StepCtl) * ctx->G);
     if (e == cudaSuccess) e = ctx->math == WR_MATH_CUDA ? configure_advance_cuda() : configure_advance_portable();
+    if (e == cudaSuccess) e = configure_advance_coop8();
+    if (e == cudaSuccess) e = configure_advance_coop16();
+    if (e == cudaSuccess) e = configure_advance_coop32();
     if (e != cudaSuccess) {
         wr_destroy(ctx);
         return fail("wr_create allocation", e);
@@ -490,6 +602,7 @@ int wr_advance(wr_ctx* ctx, int completed_global_steps, double next_grid_time, d
     k_begin_advance<<<1, 1, 0, ctx->stream>>>(ctx->ctl, completed_global_steps, next_grid_time, dt_grid);
     cudaError_t e = launch_order(ctx);
     if (e == cudaSuccess) e = launch_advance(ctx);
+    if (e == cudaSuccess) e = launch_commit(ctx);
     if (e != cudaSuccess) return fail("advance launch", e);
     rc = read_ctl(ctx);
     if (rc != WR_SUCCESS) return rc;
@@ -497,16 +610,22 @@ int wr_advance(wr_ctx* ctx, int completed_global_steps, double next_grid_time, d
     return ctx->host_ctl->failure;
 }
 
-// one outer step's launches (graph capture and the profiled path share them)
-static cudaError_t launch_step(wr_ctx* ctx) {
+// one outer step's launches (captured into the graph); with profiling on, the
+// events of chunk step `slot` bracket the prepare and the advance launch
+static cudaError_t launch_step(wr_ctx* ctx, int slot) {
+    record(ctx, 4 * slot + 0);
     cudaError_t e = launch_prepare(ctx);
+    record(ctx, 4 * slot + 1);
     if (e == cudaSuccess) {
         g_launches.fetch_add(1, std::memory_order_relaxed);
         k_decide<<<1, 1024, 0, ctx->stream>>>(ctx->ctl, ctx->G, ctx->dt_hist,
                                               ctx->policy == WR_POLICY_LEGACY_LOCAL);
         e = launch_order(ctx);
     }
+    record(ctx, 4 * slot + 2);
     if (e == cudaSuccess) e = launch_advance(ctx);
+    record(ctx, 4 * slot + 3);
+    if (e == cudaSuccess) e = launch_commit(ctx);
     if (e == cudaSuccess) {
         g_launches.fetch_add(1, std::memory_order_relaxed);
         k_finalize<<<1, 1024, 0, ctx->stream>>>(ctx->ctl, ctx->G, WR_MAX_COLLAPSE_STEPS);
@@ -516,7 +635,9 @@ static cudaError_t launch_step(wr_ctx* ctx) {
 }
 
 static int ensure_graph(wr_ctx* ctx) {
-    if (ctx->graph && ctx->graph_variant == ctx->variant && ctx->graph_policy == ctx->policy) return WR_SUCCESS;
+    if (ctx->graph && ctx->graph_variant == ctx->variant && ctx->graph_policy == ctx->policy &&
+        ctx->graph_timed == (ctx->profiling ? 1 : 0))
+        return WR_SUCCESS;
     if (ctx->graph) {
         cudaGraphExecDestroy(ctx->graph);
         ctx->graph = nullptr;
@@ -524,7 +645,7 @@ static int ensure_graph(wr_ctx* ctx) {
     const uint64_t before = g_launches.load();
     cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return fail("cudaStreamBeginCapture", e);
-    for (int i = 0; i < kCheckEvery && e == cudaSuccess; ++i) e = launch_step(ctx);
+    for (int i = 0; i < kCheckEvery && e == cudaSuccess; ++i) e = launch_step(ctx, i);
     cudaGraph_t graph = nullptr;
     const cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &graph);
     g_launches.store(before);  // capture launches nothing
@@ -537,23 +658,52 @@ static int ensure_graph(wr_ctx* ctx) {
     if (e != cudaSuccess) return fail("cudaGraphInstantiate", e);
     ctx->graph_variant = ctx->variant;
     ctx->graph_policy = ctx->policy;
+    ctx->graph_timed = ctx->profiling ? 1 : 0;
     return WR_SUCCESS;
 }
 
-// wr_run without per-kernel timing: chunks of kCheckEvery outer steps replayed
-// from a CUDA graph, one 64-byte-per-grid status read between chunks
+// wr_run: chunks of kCheckEvery outer steps replayed from a CUDA graph, one
+// 64-byte-per-grid status read between chunks.  With profiling on, the graph also
+// records an event pair around every prepare and advance launch, and an event
+// pair brackets the whole run: the per-kernel times of the shipped path.
 static int run_graph(wr_ctx* ctx, int perturb, int* completed_global_steps) {
     int rc = ensure_graph(ctx);
     if (rc != WR_SUCCESS) return rc;
+    const int nev = 4 * WR_MAX_COLLAPSE_STEPS + 2;
+    wr_run_timing t{};
+    record(ctx, nev - 2);
     g_launches.fetch_add(1, std::memory_order_relaxed);
     k_begin_run<<<1, 1024, 0, ctx->stream>>>(ctx->ctl, ctx->G, *completed_global_steps, perturb ? 1 : 0);
     for (int done = 0; done < WR_MAX_COLLAPSE_STEPS; done += kCheckEvery) {
         cudaError_t e = cudaGraphLaunch(ctx->graph, ctx->stream);
         if (e != cudaSuccess) return fail("cudaGraphLaunch", e);
-        g_launches.fetch_add(5 * kCheckEvery, std::memory_order_relaxed);
+        g_launches.fetch_add((coop_active(ctx) ? 6 : 5) * kCheckEvery, std::memory_order_relaxed);
         rc = read_ctl(ctx);
         if (rc != WR_SUCCESS) return rc;
+        if (ctx->profiling) {
+            for (int s = 0; s < kCheckEvery; ++s) {
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, ctx->ev[4 * s + 0], ctx->ev[4 * s + 1]);
+                t.prepare_ms += ms;
+                cudaEventElapsedTime(&ms, ctx->ev[4 * s + 2], ctx->ev[4 * s + 3]);
+                t.advance_ms += ms;
+            }
+        }
         if (ctx->host_ctl->all_stop) break;
+    }
+    if (ctx->profiling) {
+        record(ctx, nev - 1);
+        const cudaError_t e = cudaEventSynchronize(ctx->ev[nev - 1]);
+        if (e != cudaSuccess) return fail("cudaEventSynchronize", e);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, ctx->ev[nev - 2], ctx->ev[nev - 1]);
+        t.run_ms = ms;
+        int steps = 0;  // outer steps that advanced some grid
+        for (int g = 0; g < ctx->G; ++g) steps = ctx->host_ctl[g].cgs > steps ? ctx->host_ctl[g].cgs : steps;
+        t.advance_launches = steps;
+        t.prepare_launches = steps;
+        t.outer_steps = ctx->host_ctl->cgs;
+        ctx->timing = t;
     }
     *completed_global_steps = ctx->host_ctl->cgs;
     for (int g = 0; g < ctx->G; ++g)
@@ -567,8 +717,7 @@ int wr_run(wr_ctx* ctx, int perturb, int* completed_global_steps) {
     if (!ctx || !completed_global_steps) return fail_msg("wr_run: null argument");
     int rc = set_device(ctx);
     if (rc != WR_SUCCESS) return rc;
-    if (!ctx->profiling) return run_graph(ctx, perturb, completed_global_steps);
-    return run_profiled(ctx, perturb, WR_MAX_COLLAPSE_STEPS, completed_global_steps);
+    return run_graph(ctx, perturb, completed_global_steps);
 }
 
 // launch by launch, with CUDA events around every kernel when profiling; stops
@@ -593,6 +742,7 @@ static int run_profiled(wr_ctx* ctx, int perturb, int max_steps, int* completed_
             record(ctx, 4 * step + 2);
             if (e == cudaSuccess) e = launch_advance(ctx);
             record(ctx, 4 * step + 3);
+            if (e == cudaSuccess) e = launch_commit(ctx);
         }
         steps_launched = step + 1;
         if (e == cudaSuccess) {
@@ -705,8 +855,8 @@ int wr_set_policy(wr_ctx* ctx, int policy) {
         policy != WR_POLICY_GRIDWIDE_CTA32)
         return fail_msg("wr_set_policy: unknown policy");
     if (policy == WR_POLICY_LEGACY_LOCAL && ctx->G != 1) return fail_msg("wr_set_policy: legacy-local needs one grid");
-    if (policy == WR_POLICY_GRIDWIDE_CTA32 && (ctx->G != 1 || ctx->math != WR_MATH_PORTABLE))
-        return fail_msg("wr_set_policy: gridwide-cta32 needs one grid and portable math");
+    if (policy == WR_POLICY_GRIDWIDE_CTA32 && ctx->G != 1)
+        return fail_msg("wr_set_policy: gridwide-cta32 needs one grid");
     int rc = set_device(ctx);
     if (rc != WR_SUCCESS) return rc;
     if (policy == WR_POLICY_LEGACY_LOCAL && !ctx->local_dt) {
@@ -771,7 +921,7 @@ int wr_run_cells(wr_collapse_state* cells, int num_cells, int perturb, int* comp
     int device = 0;
     cudaGetDevice(&device);
     wr_ctx* ctx = nullptr;
-    int rc = wr_create(num_cells, device, WR_MATH_PORTABLE, &ctx);
+    int rc = wr_create(num_cells, device, WR_MATH_CUDA, &ctx);
     if (rc != WR_SUCCESS) return rc;
     rc = wr_upload(ctx, cells);
     int result = rc;

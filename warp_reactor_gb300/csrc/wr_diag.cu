@@ -5,7 +5,7 @@
 #include <string>
 
 #include "../../include/warp_reactor_diag.h"
-#include "wr_kernels.cuh"
+#include "wr_launch.h"
 
 using namespace wr;
 
@@ -178,6 +178,58 @@ int wr_diag_lu(int n, const double* A, const double* b, double* LU, int* ipvt, i
     if (e == cudaSuccess) e = cudaMemcpy(info, dinfo.p, nn * 4, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(x, dx.p, nn * 15 * 8, cudaMemcpyDeviceToHost);
     return e == cudaSuccess ? WR_SUCCESS : diag_fail("wr_diag_lu", e);
+}
+
+int wr_diag_coop_network(int lanes_per_cell, int n, const double* y, int math_mode, double* J, double* f,
+                         double* f2) {
+    if (n <= 0 || !y || !J || !f || !f2) return WR_BAD_INPUTS;
+    if (lanes_per_cell != 8 && lanes_per_cell != 16 && lanes_per_cell != 32) return WR_BAD_INPUTS;
+    const size_t nn = static_cast<size_t>(n);
+    DevBuf dy, dJ, dF, dR;
+    cudaError_t e = cudaMalloc(&dy.p, nn * NEQ * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&dJ.p, nn * NEQ * NEQ * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&dF.p, nn * NEQ * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&dR.p, nn * NEQ * 8);
+    if (e == cudaSuccess) e = cudaMemcpy(dy.p, y, nn * NEQ * 8, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return diag_fail("wr_diag_coop_network setup", e);
+    const int mc = math_mode == WR_MATH_CUDA ? 1 : 0;
+    const double* py = static_cast<const double*>(dy.p);
+    double *pJ = static_cast<double*>(dJ.p), *pF = static_cast<double*>(dF.p), *pR = static_cast<double*>(dR.p);
+    e = lanes_per_cell == 8    ? diag_coop_network8(mc, n, py, pJ, pF, pR)
+        : lanes_per_cell == 16 ? diag_coop_network16(mc, n, py, pJ, pF, pR)
+                               : diag_coop_network32(mc, n, py, pJ, pF, pR);
+    if (e == cudaSuccess) e = cudaMemcpy(J, dJ.p, nn * NEQ * NEQ * 8, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(f, dF.p, nn * NEQ * 8, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(f2, dR.p, nn * NEQ * 8, cudaMemcpyDeviceToHost);
+    return e == cudaSuccess ? WR_SUCCESS : diag_fail("wr_diag_coop_network", e);
+}
+
+int wr_diag_coop_lu(int lanes_per_cell, int n, const double* A, const double* b, double* LU, int* ipvt, int* info,
+                    double* x) {
+    if (n <= 0 || !A || !b || !LU || !ipvt || !info || !x) return WR_BAD_INPUTS;
+    if (lanes_per_cell != 8 && lanes_per_cell != 16 && lanes_per_cell != 32) return WR_BAD_INPUTS;
+    const size_t nn = static_cast<size_t>(n);
+    DevBuf dA, db, dLU, dip, dinfo, dx;
+    cudaError_t e = cudaMalloc(&dA.p, nn * 225 * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&db.p, nn * 15 * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&dLU.p, nn * 225 * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&dip.p, nn * 15 * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&dinfo.p, nn * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&dx.p, nn * 15 * 8);
+    if (e == cudaSuccess) e = cudaMemcpy(dA.p, A, nn * 225 * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(db.p, b, nn * 15 * 8, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return diag_fail("wr_diag_coop_lu setup", e);
+    const double *pA = static_cast<const double*>(dA.p), *pb = static_cast<const double*>(db.p);
+    double *pLU = static_cast<double*>(dLU.p), *px = static_cast<double*>(dx.p);
+    int *pip = static_cast<int*>(dip.p), *pinfo = static_cast<int*>(dinfo.p);
+    e = lanes_per_cell == 8    ? diag_coop_lu8(n, pA, pb, pLU, pip, pinfo, px)
+        : lanes_per_cell == 16 ? diag_coop_lu16(n, pA, pb, pLU, pip, pinfo, px)
+                               : diag_coop_lu32(n, pA, pb, pLU, pip, pinfo, px);
+    if (e == cudaSuccess) e = cudaMemcpy(LU, dLU.p, nn * 225 * 8, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(ipvt, dip.p, nn * 15 * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(info, dinfo.p, nn * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(x, dx.p, nn * 15 * 8, cudaMemcpyDeviceToHost);
+    return e == cudaSuccess ? WR_SUCCESS : diag_fail("wr_diag_coop_lu", e);
 }
 
 int wr_diag_math(int n, const double* x, int fn, int math_mode, double* out) {

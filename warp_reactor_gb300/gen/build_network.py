@@ -70,6 +70,8 @@ def emit_header(out_path: str = DEFAULT_HEADER, ir_path: str = ir_io.DEFAULT_PAT
     digest = ir_io.digest(ir_path)
     _write_if_changed(out_path, _emit.emit_header(dag, digest))
     _write_if_changed(adjoint_path, _adjoint.emit_header(dag, digest))
+    from . import coop as _coop
+    _coop.emit_all(os.path.dirname(out_path), ir_path)
     return out_path
 
 

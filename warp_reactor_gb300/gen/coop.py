@@ -1,0 +1,489 @@
+"""Vector programs of the network for the cooperative (lanes-per-cell) advance kernel.
+
+The cooperative kernel evaluates one cell's network with ``G`` lanes (``G`` = 8,
+16 or 32 lanes per cell, ``32/G`` cells per warp).  The values of the evaluation
+live in the cell's shared-memory slot array ``V``; the work is a *program*: a
+sequence of steps, each executed by every lane of the warp, in which lane ``g``
+computes one node of the DAG from operands gathered out of ``V`` (or the block's
+constant table) and stores it back into ``V``.  Between steps the warp
+synchronises, so a step may use any value produced by an earlier step.
+
+Step format (per lane, two 64-bit words):
+
+* main word: class (3 bits: none, fma, exp, log, sqrt, div), "has integer part"
+  (1 bit), destination slot (12 bits) and three operands (16 bits each);
+* integer word: op (copy, le, lt, and, or, not, sel), destination and three
+  operands.  Every step may carry up to ``G`` integer nodes beside its main node,
+  so comparisons, selects and boolean logic ride along with the floating-point
+  work instead of taking steps of their own.
+
+Operand: slot index (12 bits), "constant table" flag, negate flag and absolute
+value flag.  ``neg`` and ``abs`` nodes of the DAG are therefore never computed:
+they become operand modifiers (a sign-bit operation on the integer pipe, exact).
+
+Arithmetic: every ``add``, ``sub`` and ``mul`` is one fused multiply-add with an
+exact neutral operand, so one FP64 instruction class serves all three and lanes of
+a step may mix them.  Each is the same correctly rounded binary64 result as the
+separate operation:
+
+* ``a * b  == fma(a, b, -0.0)`` (adding -0 never changes a product, and keeps the
+  sign of a zero product);
+* ``a + b  == fma(a, 1.0, b)`` (a * 1 is exact, then one rounding of the sum);
+* ``a - b  == fma(a, 1.0, -b)`` (IEEE defines a - b as a + (-b)).
+
+Comparisons are done on the bit patterns (exact IEEE ordering: NaN unordered,
+-0 == +0), booleans are stored as the integers 0/1, selects copy bit patterns.
+
+Two programs are generated per ``G``:
+
+* ``jrhs``: inputs ``y[0..14]`` (the ROS2S state: 14 number densities and the
+  internal energy); prologue ``burn_state_from_y`` (reproducer.cpp:7029-7038):
+  ``X = max(y, 1e-100)`` and ``T = eos_re(X, e)`` (reproducer.cpp:284-314);
+  then the fused analytic Jacobian + RHS of ``network.ir``.  The Jacobian is
+  written straight into the cell's iteration matrix as ``E = -J`` (slots
+  ``r*15 + c``), the RHS values stay in slots listed in the program's output
+  table;
+* ``rhs``: the same prologue and the RHS only.
+
+Slot map of a cell: ``[0, 225)`` the iteration matrix (never used as scratch, so
+the LU factors survive the stage RHS evaluations), ``[225, 240)`` the inputs, then
+scratch values allocated by a linear scan over the schedule; the last slot is a
+write sink for idle lanes.
+
+Scheduling is list scheduling by critical path (longest weighted path to an
+output) with one class per step.  Every schedule of the DAG gives the same bits:
+each node is the same operation on the same operands wherever and whenever it is
+computed.
+"""
+from __future__ import annotations
+
+import collections
+import os
+import struct
+
+from . import ir_io
+
+# main classes
+C_NONE, C_FMA, C_EXP, C_LOG, C_SQRT, C_DIV = 0, 1, 2, 3, 4, 5
+# integer ops
+I_COPY, I_LE, I_LT, I_AND, I_OR, I_NOT, I_SEL = 0, 1, 2, 3, 4, 5, 6
+
+MAIN_CLASS = {"add": C_FMA, "sub": C_FMA, "mul": C_FMA, "exp": C_EXP, "cexp": C_EXP, "log": C_LOG,
+              "clog": C_LOG, "sqrt": C_SQRT, "csqrt": C_SQRT, "div": C_DIV}
+INT_OP = {"le": I_LE, "lt": I_LT, "and": I_AND, "or": I_OR, "not": I_NOT, "sel": I_SEL, "copy": I_COPY}
+# FP64 issue slots of one step of each class (measured call throughput of CUDA's
+# exp/log/sqrt on GB300; division runs on the integer pipe)
+STEP_COST = {C_FMA: 1.0, C_EXP: 19.0, C_LOG: 29.0, C_SQRT: 9.0, C_DIV: 0.5}
+# latency weights for the critical-path priority
+LATENCY = {C_FMA: 1.0, C_EXP: 3.0, C_LOG: 3.0, C_SQRT: 2.0, C_DIV: 2.0, "int": 1.0}
+
+E_SLOTS = 225
+Y_BASE = 225
+SLOT_BITS = 12
+MAX_SLOTS = 1 << SLOT_BITS
+OPF_CONST = 1 << 12
+OPF_NEG = 1 << 13
+OPF_ABS = 1 << 14
+
+FLOOR = 1.0e-100  # reproducer.cpp:231
+# species masses, reproducer.cpp:233-248 (the literals of wr_physics.cuh)
+MASS = (9.10938188e-28, 1.67262158e-24, 1.67353251819e-24, 1.67444345638e-24, 3.34512158e-24,
+        3.34603251819e-24, 3.34615409819e-24, 3.34694345638e-24, 3.34706503638e-24, 5.01865409819e-24,
+        5.01956503638e-24, 6.69024316e-24, 6.69115409819e-24, 6.69206503638e-24)
+K_MP = 1.67262192595e-24
+K_GAS = 6.02214076e+23 * 1.3806490000000002e-16
+
+
+def inv_gm1(n: int) -> float:
+    return 1.0 / ((1.4 if n in (6, 8, 9, 10) else 5.0 / 3.0) - 1.0)
+
+
+def dbits(v: float) -> int:
+    return struct.unpack("<Q", struct.pack("<d", v))[0]
+
+
+class Program:
+    """A DAG in program form: nodes (op, args), leaves 'in'/'const'."""
+
+    def __init__(self):
+        self.nodes = []      # (op, args); const: ('const', (bits,)); in: ('in', (k,))
+        self.cmemo = {}
+
+    def add(self, op, *args):
+        self.nodes.append((op, tuple(args)))
+        return len(self.nodes) - 1
+
+    def const_bits(self, bits: int):
+        if bits not in self.cmemo:
+            self.cmemo[bits] = self.add("const", bits)
+        return self.cmemo[bits]
+
+    def const(self, v: float):
+        return self.const_bits(dbits(v))
+
+
+def build(dag, kind: str) -> tuple:
+    """The program of ``kind`` ('jrhs' or 'rhs') and its outputs:
+    ``jac`` {(r, c): node} (jrhs only) and ``rhs`` [node] * 15."""
+    P = Program()
+    Y = [P.add("in", k) for k in range(15)]
+    floor = P.const(FLOOR)
+    # burn_state_from_y: X = smax(y, floor) = (y < floor) ? floor : y
+    X = [P.add("sel", P.add("lt", Y[k], floor), floor, Y[k]) for k in range(14)]
+    # eos_re (eos_sums + T): the sums start from 0.0, and 0.0 + v == v for the
+    # products/terms here (positive: X >= 1e-100, or NaN), so the first add is dropped
+    rhotot = P.add("mul", X[0], P.const(MASS[0]))
+    for n in range(1, 14):
+        rhotot = P.add("add", rhotot, P.add("mul", X[n], P.const(MASS[n])))
+    sa = X[0]
+    for n in range(1, 14):
+        sa = P.add("add", sa, X[n])
+    sg = None
+    for n in range(14):
+        term = P.add("mul", P.add("div", P.add("mul", X[n], P.const(K_MP)), rhotot), P.const(inv_gm1(n)))
+        sg = term if sg is None else P.add("add", sg, term)
+    sa = P.add("mul", sa, P.add("div", P.const(K_MP), rhotot))
+    sg = P.add("div", sg, sa)
+    T = P.add("div", Y[14], P.add("mul", P.add("mul", sg, P.const(K_GAS)), sa))
+    # the network with X, T substituted
+    roots = dag.rhs_roots() + (dag.jac_roots() if kind == "jrhs" else [])
+    live = dag.live_from(roots)
+    m = {}
+    for x in live:
+        n = dag.nodes[x]
+        if n.op == "in":
+            m[x] = T if n.args[0] == "T" else X[int(n.args[0][1:])]
+        elif n.op == "const":
+            m[x] = P.const(float.fromhex(n.args[0]))
+        elif n.op == "bconst":
+            m[x] = P.const_bits(1 if n.args[0] else 0)
+        else:
+            m[x] = P.add(n.op, *[m[a] for a in n.args])
+    out = {"rhs": [m[dag.outputs[("rhs", i)]] for i in range(15)]}
+    if kind == "jrhs":
+        out["jac"] = {(r, c): m[dag.outputs[("jac", r, c)]] for r in range(15) for c in range(15)}
+    return P, out
+
+
+def resolve(P: Program, x: int):
+    """(base node, neg, abs) of x with neg/abs nodes folded into modifiers."""
+    chain = []
+    while P.nodes[x][0] in ("neg", "abs"):
+        chain.append(P.nodes[x][0])
+        x = P.nodes[x][1][0]
+    neg = ab = False
+    for op in reversed(chain):  # innermost first
+        if op == "neg":
+            neg = not neg
+        else:
+            ab, neg = True, False
+    return x, neg, ab
+
+
+class Schedule:
+    def __init__(self, G, steps, slot, nv, outputs, consts):
+        self.G = G
+        self.steps = steps        # [(cls, [main node], [int node])]
+        self.slot = slot          # node -> slot
+        self.nv = nv
+        self.outputs = outputs
+        self.consts = consts
+
+
+def list_schedule(comp, args, users, kind, prio, G):
+    """Steps of width G: each step takes up to G ready nodes of one main class
+    (highest priority first; a full step is preferred) and up to G ready integer
+    nodes.  ``args``/``users`` give the dependences in the direction scheduled."""
+    pend = {x: len(set(args[x])) for x in comp}
+    ready = collections.defaultdict(list)
+    for x in comp:
+        if pend[x] == 0:
+            ready[kind(x)].append(x)
+    steps = []
+    left = len(comp)
+    mains = (C_FMA, C_EXP, C_LOG, C_SQRT, C_DIV)
+    while left:
+        rl = sorted(ready["int"], key=lambda x: -prio[x])
+        riders, ready["int"] = rl[:G], rl[G:]
+        cand = [c for c in mains if ready[c]]
+        cls, take = C_NONE, []
+        if cand:
+            full = [c for c in cand if len(ready[c]) >= G]
+            pool = full if full else cand
+            cls = max(pool, key=lambda c: (max(prio[x] for x in ready[c]), len(ready[c])))
+            rl = sorted(ready[cls], key=lambda x: -prio[x])
+            take, ready[cls] = rl[:G], rl[G:]
+        steps.append((cls, take, riders))
+        left -= len(take) + len(riders)
+        for x in take + riders:
+            for u in users[x]:
+                pend[u] -= 1
+                if pend[u] == 0:
+                    ready[kind(u)].append(u)
+    return steps
+
+
+def schedule(P: Program, out: dict, G: int, copy_jac: bool, reverse: bool = False):
+    """List-schedule the program into steps of width G and allocate slots.
+
+    ``reverse``: schedule from the outputs back to the inputs (each node as late
+    as its users allow, by depth from the inputs) and reverse the step list.
+    Values are then computed shortly before they are used, which keeps the live
+    set (the shared memory per cell) small at the same step count; forward
+    scheduling by critical path computes values as early as possible."""
+    leaf = ("in", "const")
+    # pseudo nodes: E(r,c) = -J(r,c) copies into the matrix slots
+    copies = []
+    if copy_jac:
+        for (r, c), x in sorted(out["jac"].items()):
+            copies.append((P.add("copy", x), r * 15 + c))
+    roots = list(out["rhs"]) + [cp for cp, _ in copies]
+    # live compute nodes (neg/abs folded)
+    seen, stack = set(), [resolve(P, r)[0] for r in roots]
+    while stack:
+        x = stack.pop()
+        if x in seen:
+            continue
+        seen.add(x)
+        op, a = P.nodes[x]
+        if op in leaf:
+            continue
+        for y in a:
+            stack.append(resolve(P, y)[0])
+    comp = sorted(x for x in seen if P.nodes[x][0] not in leaf)
+    args = {x: [resolve(P, a)[0] for a in P.nodes[x][1]] for x in comp}
+    cargs = {x: sorted({a for a in args[x] if P.nodes[a][0] not in leaf}) for x in comp}
+    users = collections.defaultdict(list)
+    for x in comp:
+        for a in cargs[x]:
+            users[a].append(x)
+
+    def kind(x):
+        return MAIN_CLASS.get(P.nodes[x][0], "int")
+
+    if reverse:
+        depth = {}
+        for x in comp:
+            depth[x] = LATENCY[kind(x)] + max((depth[a] for a in cargs[x]), default=0.0)
+        rsteps = list_schedule(comp, {x: users[x] for x in comp}, cargs, kind, depth, G)
+        steps = rsteps[::-1]
+    else:
+        prio = {}
+        for x in reversed(comp):
+            prio[x] = LATENCY[kind(x)] + max((prio[u] for u in users[x]), default=0.0)
+        steps = list_schedule(comp, cargs, users, kind, prio, G)
+    done_at = {}
+    for s, (cls, take, riders) in enumerate(steps):
+        for x in take + riders:
+            done_at[x] = s
+    for x in comp:
+        assert all(done_at[a] < done_at[x] for a in cargs[x]), "schedule violates a dependence"
+    # ---- slot allocation (linear scan; a slot read last in step s is free from s+1)
+    last = {}
+    for s, (cls, take, riders) in enumerate(steps):
+        for x in take + riders:
+            for a in args[x]:
+                if P.nodes[a][0] == "in" or P.nodes[a][0] not in leaf:
+                    last[a] = s
+    end = len(steps)
+    keep = {resolve(P, r)[0] for r in out["rhs"]}
+    slot = {}
+    inputs = [x for x in range(len(P.nodes)) if P.nodes[x][0] == "in"]
+    for x in inputs:
+        slot[x] = Y_BASE + P.nodes[x][1][0]
+    copy_dst = dict(copies)
+    free = []  # min-heap of free scratch slots
+    import heapq
+    next_slot = Y_BASE + 15
+    release = collections.defaultdict(list)
+    for x in inputs:
+        if x in last:
+            release[last[x] + 1].append(slot[x])
+        else:
+            heapq.heappush(free, slot[x])
+    nv = next_slot
+    for s, (cls, take, riders) in enumerate(steps):
+        for sl in release.pop(s, []):
+            heapq.heappush(free, sl)
+        for x in take + riders:
+            if x in copy_dst:
+                slot[x] = copy_dst[x]
+                continue
+            if free:
+                sl = heapq.heappop(free)
+            else:
+                sl = next_slot
+                next_slot += 1
+            slot[x] = sl
+            if x not in keep:
+                release[last.get(x, s) + 1].append(sl)
+        nv = max(nv, next_slot)
+    nv += 1  # write sink of idle lanes
+    if nv > MAX_SLOTS:
+        raise ValueError(f"program needs {nv} slots (max {MAX_SLOTS})")
+    outputs = {"rhs": [resolve(P, r) for r in out["rhs"]]}
+    return Schedule(G, steps, slot, nv, outputs, None), args
+
+
+def encode(P: Program, sch: Schedule, args, cidx: dict, sink: int, one: int, mzero: int):
+    """Per-step, per-lane (main, int) words."""
+    G = sch.G
+
+    def operand(x, neg=False, ab=False):
+        b, n2, a2 = resolve(P, x)
+        # compose the caller's modifiers outside the node's own chain
+        if ab:
+            n2, a2 = False, True
+        if neg:
+            n2 = not n2
+        if P.nodes[b][0] == "const":
+            v = cidx[P.nodes[b][1][0]] | OPF_CONST
+        else:
+            v = sch.slot[b]
+        return v | (OPF_NEG if n2 else 0) | (OPF_ABS if a2 else 0)
+
+    c_one = cidx[one] | OPF_CONST
+    c_mzero = cidx[mzero] | OPF_CONST
+    words = []
+    for cls, take, riders in sch.steps:
+        lanes = []
+        for g in range(G):
+            if g < len(take):
+                x = take[g]
+                op, a = P.nodes[x]
+                if op == "mul":
+                    p, q, s = operand(a[0]), operand(a[1]), c_mzero
+                elif op == "add":
+                    p, q, s = operand(a[0]), c_one, operand(a[1])
+                elif op == "sub":
+                    p, q, s = operand(a[0]), c_one, operand(a[1], neg=True)
+                elif op == "div":
+                    p, q, s = operand(a[0]), operand(a[1]), c_one
+                else:  # exp, log, sqrt (and their constant-argument forms)
+                    p, q, s = operand(a[0]), c_one, c_one
+                dst = sch.slot[x]
+            else:
+                p = q = s = c_one
+                dst = sink
+            hi = (cls << 60) | ((1 << 63) if riders else 0)
+            main = hi | (dst << 48) | (s << 32) | (q << 16) | p
+            if g < len(riders):
+                x = riders[g]
+                op, a = P.nodes[x]
+                iop = INT_OP[op]
+                if op == "copy":  # E = -J
+                    ops = [operand(a[0], neg=True), c_one, c_one]
+                elif op == "not":
+                    ops = [operand(a[0]), c_one, c_one]
+                elif op == "sel":
+                    ops = [operand(a[0]), operand(a[1]), operand(a[2])]
+                else:
+                    ops = [operand(a[0]), operand(a[1]), c_one]
+                idst = sch.slot[x]
+            else:
+                iop, ops, idst = I_COPY, [c_one, c_one, c_one], sink
+            iw = (iop << 60) | (idst << 48) | (ops[2] << 32) | (ops[1] << 16) | ops[0]
+            lanes.append((main, iw))
+        words.append(lanes)
+    return words
+
+
+def generate(G: int, dag=None):
+    """Programs jrhs and rhs for G lanes per cell: a dict with the encoded steps,
+    the output operands, the slot count and the constant table."""
+    dag = dag or ir_io.load()
+    progs = {}
+    consts = set()
+    built = {}
+    for kind in ("jrhs", "rhs"):
+        P, out = build(dag, kind)
+        sch, args = schedule(P, out, G, copy_jac=(kind == "jrhs"))
+        built[kind] = (P, out, sch, args)
+        for x in range(len(P.nodes)):
+            if P.nodes[x][0] == "const":
+                consts.add(P.nodes[x][1][0])
+    one, mzero = dbits(1.0), dbits(-0.0)
+    consts |= {one, mzero}
+    ctab = sorted(consts)
+    cidx = {b: i for i, b in enumerate(ctab)}
+    if len(ctab) > MAX_SLOTS:
+        raise ValueError("constant table too large")
+    nv = max(b[2].nv for b in built.values())
+    sink = nv - 1
+    for kind, (P, out, sch, args) in built.items():
+        words = encode(P, sch, args, cidx, sink, one, mzero)
+
+        def outop(r):
+            b, neg, ab = r
+            v = (cidx[P.nodes[b][1][0]] | OPF_CONST) if P.nodes[b][0] == "const" else sch.slot[b]
+            return v | (OPF_NEG if neg else 0) | (OPF_ABS if ab else 0)
+
+        progs[kind] = {"words": words, "rhs_out": [outop(r) for r in sch.outputs["rhs"]],
+                       "nsteps": len(sch.steps), "stats": stats(sch)}
+    return {"G": G, "nv": nv, "consts": ctab, "progs": progs}
+
+
+def stats(sch: Schedule) -> dict:
+    cnt = collections.Counter(c for c, _, _ in sch.steps)
+    cost = sum(STEP_COST.get(c, 0.0) for c, _, _ in sch.steps)
+    return {"steps": len(sch.steps), "by_class": {str(k): v for k, v in sorted(cnt.items())},
+            "fp64_slots": cost, "slots": sch.nv}
+
+
+def emit_header(G: int, gen: dict, digest: str) -> str:
+    lines = [
+        "// Generated by warp_reactor_gb300/gen/coop.py from network.ir",
+        f"// network.ir sha256 {digest}",
+        f"// Vector programs of the network for {G} lanes per cell.",
+        "#pragma once",
+        "#include <stdint.h>",
+        "",
+        f"namespace wr {{ namespace coop{G} {{",
+        f"constexpr int kG = {G};",
+        f"constexpr int kNV = {gen['nv']};",
+        f"constexpr int kNC = {len(gen['consts'])};",
+    ]
+    for kind, pr in gen["progs"].items():
+        st = pr["stats"]
+        lines.append(f"constexpr int k{kind.upper()}Steps = {pr['nsteps']};  // {st['by_class']}, "
+                     f"{st['fp64_slots']:.0f} FP64 issue slots")
+    lines.append("")
+    lines.append("static __device__ const uint64_t kConst[kNC] = {")
+    cs = gen["consts"]
+    for i in range(0, len(cs), 4):
+        lines.append("    " + ", ".join(f"0x{b:016x}ULL" for b in cs[i:i + 4]) + ",")
+    lines.append("};")
+    for kind, pr in gen["progs"].items():
+        K = kind.upper()
+        lines.append(f"static __device__ const ulonglong2 k{K}Prog[k{K}Steps * kG] = {{")
+        for lanes in pr["words"]:
+            lines.append("    " + ", ".join(f"{{0x{m:x}ULL, 0x{i:x}ULL}}" for m, i in lanes) + ",")
+        lines.append("};")
+        lines.append(f"static __device__ const uint16_t k{K}Out[15] = {{" +
+                     ", ".join(str(v) for v in pr["rhs_out"]) + "};")
+    lines.append(f"}} }}  // namespace wr::coop{G}")
+    return "\n".join(lines) + "\n"
+
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GEN_DIR = os.path.join(os.path.dirname(HERE), "csrc", "generated")
+LANES_PER_CELL = (8, 16, 32)
+
+
+def emit_all(out_dir: str = GEN_DIR, ir_path: str = ir_io.DEFAULT_PATH) -> list:
+    from .build_network import _write_if_changed
+    dag = ir_io.load(ir_path)
+    digest = ir_io.digest(ir_path)
+    paths = []
+    for G in LANES_PER_CELL:
+        path = os.path.join(out_dir, f"coop_prog_g{G}.h")
+        _write_if_changed(path, emit_header(G, generate(G, dag), digest))
+        paths.append(path)
+    return paths
+
+
+if __name__ == "__main__":
+    d = ir_io.load()
+    for G in LANES_PER_CELL:
+        g = generate(G, d)
+        print(G, g["nv"], len(g["consts"]), {k: v["stats"] for k, v in g["progs"].items()})
