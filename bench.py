@@ -231,11 +231,13 @@ def precision_form(wr, device, math_mode, grid=16, steps=300):
     }
 
 
-def cta32_form(wr, device, math_mode, cells0, independent_run_ms, independent_cells):
+def cta32_form(wr, device, math_mode, cells0, independent_run_ms, independent_cells, grid, with_reference):
     """The reference's other GPU policy, gridwide-structured-cta32 (one ROS2S
     controller per 32-cell tile), on the bench's own grid: device time of wr_run
     with the state resident (L2 flushed), against the gridwide-independent time and
-    final state just measured; cell-attempts and how far the final states differ."""
+    final state just measured; cell-attempts and how far the final states differ.
+    With ``with_reference``, the reference's own structured kernel on the same grid
+    beside it (its time, and whether its final states equal this policy's)."""
     c = cells0.copy()
     with wr.Context(len(c), device, math_mode) as ctx:
         ctx.set_policy(wr.POLICY_GRIDWIDE_CTA32)
@@ -247,7 +249,8 @@ def cta32_form(wr, device, math_mode, cells0, independent_run_ms, independent_ce
         ctx.download(c)
     ci = independent_cells
     rT = np.abs(c["T"] / ci["T"] - 1)
-    return {"workload": "the bench grid, full collapse", "result": int(rc),
+    ref = reference_cuda_form(wr, grid, wr.pack_final_states(c, grid), structured=True) if with_reference else None
+    return {"workload": "the bench grid, full collapse", "result": int(rc), "reference_structured_kernel": ref,
             "cta32_cells_per_s": len(c) / (t.run_ms / 1e3),
             "independent_cells_per_s": len(c) / (independent_run_ms / 1e3),
             "cta32_over_independent_time": t.run_ms / independent_run_ms,
@@ -290,27 +293,31 @@ def error_table(wr, cells, ref):
             "rejected_delta": a["rejected_exact"] - r["rejected_exact"]}
 
 
-def reference_cuda_form(wr, grid, packed_ours):
+def reference_cuda_form(wr, grid, packed_ours, structured=False):
     """The reference's own CUDA kernels (prepare_grid_timestep_kernel and
     advance_collapse_gridwide_kernel, reproducer.cpp:7696-7785, compiled unmodified
-    for sm_103a) on the same grid and GPU, through the reference's host loop
-    (oracle/ref_cuda_launcher.cpp): wall time, cells/s, substep totals, and whether
-    its final_states file equals this library's final states byte for byte."""
+    for sm_103a; with ``structured`` its gridwide-structured-cta32 kernel,
+    structured_cuda.cuh:393-782) on the same grid and GPU, through the reference's
+    host loop (oracle/ref_cuda_launcher.cpp): wall time, cells/s, substep totals,
+    and whether its final_states file equals this library's final states (of the
+    same policy) byte for byte."""
     import tempfile
     from warp_reactor_gb300 import build
     exe = build.ref_cuda_launcher()
-    cubin = os.path.join(ROOT, "oracle", "_ref", "ref_kernels.cubin")
+    cubin = os.path.join(ROOT, "oracle", "_ref", "ref_structured.cubin" if structured else "ref_kernels.cubin")
     if not exe or not os.path.exists(cubin):
-        return {"unavailable": "the reference's CUDA kernels were not built (oracle/_ref/ref_kernels.cubin, "
-                               "made where the reference tree exists)"}
+        return {"unavailable": f"the reference's CUDA kernels were not built ({os.path.relpath(cubin, ROOT)}, made "
+                               "where the reference tree exists)"}
     with tempfile.TemporaryDirectory() as tmp:
         out = os.path.join(tmp, f"final_states_grid{grid}_cuda.bin")
-        r = subprocess.run([exe, cubin, str(grid), out], capture_output=True, text=True)
+        r = subprocess.run([exe, cubin, str(grid), out] + (["--structured"] if structured else []),
+                           capture_output=True, text=True)
         if r.returncode != 0:
             return {"unavailable": f"launcher exited {r.returncode}: {r.stderr.strip()[-200:]}"}
         line = json.loads(r.stdout.strip().splitlines()[-1])
         ref = np.fromfile(out, wr.PACKED_FINAL_STATE)
-    line["kind"] = "the reference's CUDA kernels, one thread per cell, 128 per block, its host loop"
+    line["kind"] = ("the reference's structured CUDA kernel, one 256-thread block per 32-cell tile, its host loop"
+                    if structured else "the reference's CUDA kernels, one thread per cell, 128 per block, its host loop")
     line["final_states_equal_bytes"] = packed_ours.tobytes() == ref.tobytes()
     if not line["final_states_equal_bytes"]:
         rT = np.abs(packed_ours["T"] - ref["T"]) / np.abs(ref["T"])
@@ -570,8 +577,9 @@ def run_gb300(args, rank, ws, local, tdist):
             forms["reference_cuda_kernel"] = reference_cuda_form(wr, grid, packed)
         if math_mode == wr.MATH_CUDA and budget_ok("portable_math", 1.5 * step_s + 10):
             forms["portable_math"] = portable_form(wr, local, cells0, out, timings[-1].run_ms)
-        if budget_ok("cta32_policy", 2.0 * step_s + 10):
-            forms["cta32_policy"] = cta32_form(wr, local, math_mode, cells0, timings[-1].run_ms, out)
+        if budget_ok("cta32_policy", 2.0 * step_s + 100):
+            forms["cta32_policy"] = cta32_form(wr, local, math_mode, cells0, timings[-1].run_ms, out, grid,
+                                               math_mode == wr.MATH_CUDA)
         if budget_ok("differentiation", 60.0):
             forms["differentiation"] = diff_measure(args.diff_grid)
         if budget_ok("batching", 150.0 * args.forms_batch_scale ** 3 + 30):

@@ -9,6 +9,9 @@ module; the GPU library never does.
                    library's default arithmetic)
 ``load("libm")``   oracle with the C library's exp/log/cbrt (the reference CPU
                    build's arithmetic)
+``load("prec")``   the precision form's arithmetic (FP32 factorisation in
+                   error-weighted variables, one FP64 residual sweep per stage
+                   solve; portable exp/log), the checker of advance variant 3
 ``load("ref")``    the reference compiled from its own sources (only where the
                    reference tree was present at build time)
 ``load_diff()``    the differentiation form's map with a frozen controller and its
@@ -25,6 +28,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PATHS = {
     "port": os.path.join(HERE, "_build", "libwr_oracle_port.so"),
     "libm": os.path.join(HERE, "_build", "libwr_oracle_libm.so"),
+    "prec": os.path.join(HERE, "_build", "libwr_oracle_prec.so"),
     "ref": os.path.join(HERE, "_ref", "libwr_ref.so"),
     "diff": os.path.join(HERE, "_build", "libwr_oracle_diff.so"),
 }

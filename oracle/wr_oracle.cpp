@@ -245,6 +245,89 @@ constexpr double kE3 = -0.13807118745769906;
 
 struct Counters { int n_step = 0, n_rhs = 0, n_jac = 0, n_accept = 0, n_reject = 0, n_decomp = 0, n_solve = 0; };
 
+// ---------------------------------------------------------------- precision form
+// WR_ORACLE_PREC (compile-time, default 0 = plain FP64): the precision form's
+// linear algebra restated from the device kernel (advance variant 3).
+//  2  the precision form (libwr_oracle_prec.so): the iteration matrix in
+//     error-weighted variables, E' = W^-1 E W with W = diag(atol + rtol |y|) (the
+//     scale of the controller's error norm, reproducer.cpp:7194-7202), rounded to
+//     FP32 and factorised in FP32 (fmaf updates); each stage solve is
+//     x0 = W LU32^-1 W^-1 b followed by WR_ORACLE_PREC_SWEEPS (default 1) FP64
+//     residual sweeps r = b - E x0 (E = fac I - J in FP64), x0 += W LU32^-1 W^-1 r;
+//  1  the same without the weights (W = I): the unscaled variant, kept to
+//     reproduce the measurement that motivated the weights.
+#ifndef WR_ORACLE_PREC
+#define WR_ORACLE_PREC 0
+#endif
+#ifndef WR_ORACLE_PREC_SWEEPS
+#define WR_ORACLE_PREC_SWEEPS 1
+#endif
+#if WR_ORACLE_PREC
+int lu_decomposition_f32(float A[NEQ][NEQ], int* ipvt) {
+    int info = 0;
+    for (int k = 0; k < NEQ - 1; ++k) {
+        int p = k;
+        float max_val = std::fabs(A[k][k]);
+        for (int i = k + 1; i < NEQ; ++i) {
+            const float v = std::fabs(A[i][k]);
+            if (v > max_val) { max_val = v; p = i; }
+        }
+        ipvt[k] = p;
+        if (A[p][k] != 0.0f) {
+            if (p != k)
+                for (int j = k; j < NEQ; ++j) { const float t = A[p][j]; A[p][j] = A[k][j]; A[k][j] = t; }
+            const float mult = -1.0f / A[k][k];
+            for (int i = k + 1; i < NEQ; ++i) A[i][k] = A[i][k] * mult;
+            for (int j = k + 1; j < NEQ; ++j) {
+                const float t = A[k][j];
+                for (int i = k + 1; i < NEQ; ++i) A[i][j] = std::fmaf(t, A[i][k], A[i][j]);
+            }
+        } else {
+            info = k + 1;
+        }
+    }
+    ipvt[NEQ - 1] = NEQ - 1;
+    if (A[NEQ - 1][NEQ - 1] == 0.0f) info = NEQ;
+    return info;
+}
+
+void lu_solve_f32(const float LU[NEQ][NEQ], const int* ipvt, float* x) {
+    for (int k = 0; k < NEQ - 1; ++k) {
+        const int p = ipvt[k];
+        const float t = x[p];
+        if (p != k) { x[p] = x[k]; x[k] = t; }
+        for (int j = k + 1; j < NEQ; ++j) x[j] = std::fmaf(t, LU[j][k], x[j]);
+    }
+    for (int kb = 0; kb < NEQ; ++kb) {
+        const int k = NEQ - 1 - kb;
+        x[k] = x[k] / LU[k][k];
+        const float t = -x[k];
+        for (int j = 0; j < k; ++j) x[j] = std::fmaf(t, LU[j][k], x[j]);
+    }
+}
+
+// x <- E^-1 x (E = fac I - J) with the FP32 factors of W^-1 E W (W = I in mode 1)
+void solve_refined(const float LU[NEQ][NEQ], const int* ip, const double J[NEQ][NEQ], double fac,
+                   const double* w, double* x) {
+    double b[NEQ], xx[NEQ];
+    for (int i = 0; i < NEQ; ++i) b[i] = x[i];
+    float xf[NEQ];
+    for (int i = 0; i < NEQ; ++i) xf[i] = static_cast<float>(b[i] / w[i]);
+    lu_solve_f32(LU, ip, xf);
+    for (int i = 0; i < NEQ; ++i) xx[i] = static_cast<double>(xf[i]) * w[i];
+    for (int sweep = 0; sweep < WR_ORACLE_PREC_SWEEPS; ++sweep) {
+        for (int i = 0; i < NEQ; ++i) {
+            double acc = 0.0;
+            for (int j = 0; j < NEQ; ++j) acc = acc + J[i][j] * xx[j];
+            xf[i] = static_cast<float>((b[i] - (fac * xx[i] - acc)) / w[i]);
+        }
+        lu_solve_f32(LU, ip, xf);
+        for (int i = 0; i < NEQ; ++i) xx[i] = xx[i] + static_cast<double>(xf[i]) * w[i];
+    }
+    for (int i = 0; i < NEQ; ++i) x[i] = xx[i];
+}
+#endif
+
 // RODAS<PrimordialChem>::integrate with configure_ros2s settings
 // (reproducer.cpp:7205-7347, 7582-7590, RODASState defaults :7077-7109).
 // y: in/out 15-vector; t from 0 to tout; returns IntegratorResult.
@@ -268,6 +351,13 @@ int ros2s_integrate(double* y, double tout, double dt0, Counters& c) {
     int n_step = 0, n_accept = 0;
     double fjac[NEQ][NEQ], e[NEQ][NEQ];
     int ip[NEQ];
+#if WR_ORACLE_PREC
+    float e32[NEQ][NEQ];
+    double wsc[NEQ];
+#define WR_SOLVE(v) solve_refined(e32, ip, fjac, fac, wsc, v)
+#else
+#define WR_SOLVE(v) lu_solve(e, ip, v)
+#endif
     double ynew[NEQ], ak1[NEQ], ak2[NEQ], work[NEQ], dy[NEQ];
 
     for (;;) {
@@ -284,7 +374,14 @@ int ros2s_integrate(double* y, double tout, double dt0, Counters& c) {
                 for (int j = 0; j < NEQ; ++j) e[i][j] = -fjac[i][j];
                 e[i][i] += fac;
             }
+#if WR_ORACLE_PREC
+            for (int i = 0; i < NEQ; ++i) wsc[i] = WR_ORACLE_PREC == 2 ? atol[i] + rtol[i] * std::fabs(y[i]) : 1.0;
+            for (int i = 0; i < NEQ; ++i)
+                for (int j = 0; j < NEQ; ++j) e32[i][j] = static_cast<float>(e[i][j] * wsc[j] / wsc[i]);
+            const int info = lu_decomposition_f32(e32, ip);
+#else
             const int info = lu_decomposition(e, ip);
+#endif
             if (info != 0) {
                 nsing += 1;
                 if (nsing >= 5) return WR_LU_DECOMPOSITION_ERROR;
@@ -295,7 +392,7 @@ int ros2s_integrate(double* y, double tout, double dt0, Counters& c) {
             }
             c.n_decomp += 1;
             rhs(y, ak1);
-            lu_solve(e, ip, ak1);
+            WR_SOLVE(ak1);
             c.n_solve += 1;
             for (int i = 0; i < NEQ; ++i) {
                 ynew[i] = y[i] + kA21 * ak1[i];
@@ -303,7 +400,7 @@ int ros2s_integrate(double* y, double tout, double dt0, Counters& c) {
             }
             rhs(ynew, dy);
             for (int i = 0; i < NEQ; ++i) ak2[i] += dy[i];
-            lu_solve(e, ip, ak2);
+            WR_SOLVE(ak2);
             c.n_solve += 1;
             for (int i = 0; i < NEQ; ++i) {
                 ynew[i] = y[i] + kA31 * ak1[i] + kA32 * ak2[i];
@@ -311,7 +408,7 @@ int ros2s_integrate(double* y, double tout, double dt0, Counters& c) {
             }
             rhs(ynew, dy);
             for (int i = 0; i < NEQ; ++i) work[i] += dy[i];
-            lu_solve(e, ip, work);
+            WR_SOLVE(work);
             c.n_solve += 1;
             for (int i = 0; i < NEQ; ++i) {
                 const double ak3 = work[i];

@@ -39,6 +39,12 @@ def oracle_port(built):
 
 
 @pytest.fixture(scope="session")
+def oracle_prec(built):
+    from oracle import oracle
+    return oracle.load("prec")
+
+
+@pytest.fixture(scope="session")
 def oracle_libm(built):
     from oracle import oracle
     return oracle.load("libm")

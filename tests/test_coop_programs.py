@@ -17,7 +17,7 @@ import pytest
 from warp_reactor_gb300.gen import coop, ir_io
 
 C_NONE, C_FMA, C_EXP, C_LOG, C_SQRT, C_DIV = range(6)
-I_COPY, I_LE, I_LT, I_AND, I_OR, I_NOT, I_SEL = range(7)
+I_SEL, I_LE, I_LT = range(3)
 SIGN = 1 << 63
 ABS = SIGN - 1
 
@@ -75,8 +75,7 @@ def run(words, V, C, oracle, one, mzero):
                 reads.update(o & 0xfff for o in ops if not o & 0x1000)
                 A, B, Cc = (fetch(V, C, o) for o in ops)
                 fa, fb = d(A), d(B)
-                r = {I_COPY: A, I_LE: int(fa <= fb), I_LT: int(fa < fb), I_AND: A & B, I_OR: A | B,
-                     I_NOT: A ^ 1, I_SEL: B if A else Cc}[iop]
+                r = {I_LE: int(fa <= fb), I_LT: int(fa < fb), I_SEL: B if A else Cc}[iop]
                 results.append(((iw >> 48) & 0xfff, r))
         sink = len(V) - 1
         for dst, r in results:

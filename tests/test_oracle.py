@@ -182,3 +182,18 @@ def test_cta32_tiles_share_one_controller(oracle_port, count):
             assert (tile[f] == tile[f][0]).all()
     assert np.abs(b["T"] / a["T"] - 1).max() < 1e-4
     assert (b["completed_steps"] == a["completed_steps"]).all()
+
+
+def test_precision_oracle_bounded(oracle_prec, oracle_port):
+    """The precision form's arithmetic (FP32 factorisation in error-weighted
+    variables, one FP64 residual sweep) integrates the grid-1 collapse: more
+    attempts than FP64 but within 3x (unweighted FP32 factors take ~50x), and a
+    final T within 1e-3 of the FP64 oracle."""
+    a = oracle_prec.make_grid(1)
+    b = oracle_port.make_grid(1)
+    rc_a, cgs_a = oracle_prec.run(a)
+    rc_b, cgs_b = oracle_port.run(b)
+    assert rc_a == rc_b == 1 and cgs_a == cgs_b == 438
+    att_a, att_b = int(a["stats"]["internal_steps"].sum()), int(b["stats"]["internal_steps"].sum())
+    assert att_b < att_a < 3 * att_b
+    assert abs(a["T"][0] / b["T"][0] - 1) < 1e-3

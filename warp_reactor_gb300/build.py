@@ -7,6 +7,7 @@ All outputs are written in-tree and git-ignored:
   warp_reactor_gb300/_build/reproducer_gb300         the drop-in CLI
   oracle/_build/libwr_oracle_port.so                 CPU oracle, portable math
   oracle/_build/libwr_oracle_libm.so                 CPU oracle, C-library math
+  oracle/_build/libwr_oracle_prec.so                 CPU oracle, the precision form's arithmetic
 
 Translation units compile in parallel; a unit is rebuilt only when one of its
 inputs is newer than its object.  No cmake: nvcc and g++ are driven directly.
@@ -126,7 +127,8 @@ def build_oracle(verbose=False) -> list:
             os.path.join(CSRC, "generated", "network_gen.h"), os.path.join(INCLUDE, "warp_reactor.h")]
     outs = []
     tasks = []
-    for name, defs in (("libwr_oracle_port.so", []), ("libwr_oracle_libm.so", ["-DWR_ORACLE_LIBM"])):
+    for name, defs in (("libwr_oracle_port.so", []), ("libwr_oracle_libm.so", ["-DWR_ORACLE_LIBM"]),
+                       ("libwr_oracle_prec.so", ["-DWR_ORACLE_PREC=2"])):
         so = os.path.join(ORACLE_OUT, name)
         outs.append(so)
         if _stale(so, deps):

@@ -326,8 +326,17 @@ int set_device(wr_ctx* ctx) {
     return e == cudaSuccess ? WR_SUCCESS : fail("cudaSetDevice", e);
 }
 
+// with profiling on, record event idx on the context stream; inside a stream
+// capture the record becomes an event-record node of the graph (the external
+// flag, valid only during capture), so the events time the replayed kernels
 void record(wr_ctx* ctx, int idx) {
-    if (ctx->profiling) cudaEventRecord(ctx->ev[idx], ctx->stream);
+    if (!ctx->profiling) return;
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(ctx->stream, &st);
+    if (st == cudaStreamCaptureStatusActive)
+        cudaEventRecordWithFlags(ctx->ev[idx], ctx->stream, cudaEventRecordExternal);
+    else
+        cudaEventRecord(ctx->ev[idx], ctx->stream);
 }
 
 // the cooperative advance runs between k_order_preburn and k_commit

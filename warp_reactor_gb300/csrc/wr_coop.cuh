@@ -50,7 +50,7 @@ constexpr int kQBurnOK = -4;   // burned successfully: k_commit commits it
 namespace coop {
 
 enum { C_NONE = 0, C_FMA = 1, C_EXP = 2, C_LOG = 3, C_SQRT = 4, C_DIV = 5 };
-enum { I_COPY = 0, I_LE = 1, I_LT = 2, I_AND = 3, I_OR = 4, I_NOT = 5, I_SEL = 6 };
+enum { I_SEL = 0, I_LE = 1, I_LT = 2 };
 constexpr int kE = 0;        // iteration matrix slots [0, 225)
 constexpr int kY = 225;      // program inputs y[0..14]
 constexpr uint64_t kSign = 0x8000000000000000ULL;
@@ -67,6 +67,31 @@ __device__ __forceinline__ uint64_t fetch(const uint64_t* V, const uint64_t* C, 
     v = (op & 0x4000u) ? (v & kAbs) : v;
     v = (op & 0x2000u) ? (v ^ kSign) : v;
     return v;
+}
+
+// Shared-memory access by 32-bit shared-window addresses (the interpreter runs out
+// of line, where generic pointers would lose their address space).
+__device__ __forceinline__ uint64_t lds64(uint32_t addr) {
+    uint64_t v;
+    asm volatile("ld.shared.b64 %0, [%1];" : "=l"(v) : "r"(addr));
+    return v;
+}
+__device__ __forceinline__ void sts64(uint32_t addr, uint64_t v) {
+    asm volatile("st.shared.b64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
+}
+__device__ __forceinline__ void group_sync(unsigned gmask) {
+    asm volatile("bar.warp.sync %0;" ::"r"(gmask) : "memory");
+}
+// operand fetch on shared-window addresses: the slot's byte offset in the cell's
+// slot array or the constant table, then the sign modifiers on the high word
+// (abs clears bit 63, negate flips it)
+__device__ __forceinline__ uint64_t fetch_s(uint32_t vb, uint32_t cb, uint32_t op) {
+    const uint32_t addr = ((op & 0x1000u) ? cb : vb) + ((op & 0xfffu) << 3);
+    const uint64_t v = lds64(addr);
+    const uint32_t lo = static_cast<uint32_t>(v);
+    uint32_t hi = static_cast<uint32_t>(v >> 32);
+    hi = (hi & ~((op << 17) & 0x80000000u)) ^ ((op << 18) & 0x80000000u);
+    return (static_cast<uint64_t>(hi) << 32) | lo;
 }
 
 // IEEE a <= b and a < b on bit patterns: false when either is NaN, -0 == +0
@@ -87,8 +112,8 @@ __device__ __forceinline__ uint64_t blt(uint64_t a, uint64_t b) {
     return (!nan && !zero && (sa != sb ? sa : same)) ? 1ULL : 0ULL;
 }
 
-// Transcendental and division steps call one out-of-line copy each, so the
-// unrolled program loop stays small (CUDA's own functions inside for CudaMath).
+// Transcendental steps call one out-of-line copy each, so the interpreter loop
+// stays small (CUDA's own functions inside for CudaMath).
 template <class M>
 struct StepMath {
     static __device__ __noinline__ double exp(double x) { return M::exp(x); }
@@ -96,71 +121,85 @@ struct StepMath {
     static __device__ __noinline__ double sqrt(double x) { return M::sqrt(x); }
 };
 
-// Steps whose table entries are in flight ahead of the one executing: the tables
-// (~100-200 KB per G) live in L2 behind a shared-memory carve-out that leaves
-// little L1, so each entry is loaded this many steps before it is used.
-constexpr int kPrefetch = 8;
-
 template <class M>
-__device__ __forceinline__ void exec_step(const ulonglong2 e, uint64_t* V, const uint64_t* C) {
+__device__ __forceinline__ void exec_step(const ulonglong2 e, uint32_t vb, uint32_t cb) {
     const uint64_t mw = e.x;
-    const uint32_t cls = static_cast<uint32_t>(mw >> 60) & 7u;
-    if (cls != C_NONE) {
-        const double a = dbl(fetch(V, C, static_cast<uint32_t>(mw) & 0xffffu));
-        const double b = dbl(fetch(V, C, static_cast<uint32_t>(mw >> 16) & 0xffffu));
+    const uint32_t lo = static_cast<uint32_t>(mw), hi = static_cast<uint32_t>(mw >> 32);
+    const uint32_t cls = (hi >> 28) & 7u;
+    if (cls == C_FMA) {
+        const double a = dbl(fetch_s(vb, cb, lo & 0x7fffu));
+        const double b = dbl(fetch_s(vb, cb, lo >> 16));
+        const double c = dbl(fetch_s(vb, cb, hi & 0xffffu));
+        sts64(vb + (((hi >> 16) & 0xfffu) << 3), bits(__fma_rn(a, b, c)));
+    } else if (cls != C_NONE) {
+        const double a = dbl(fetch_s(vb, cb, lo & 0x7fffu));
         double r;
-        if (cls == C_FMA) {
-            r = __fma_rn(a, b, dbl(fetch(V, C, static_cast<uint32_t>(mw >> 32) & 0xffffu)));
+        if (cls == C_DIV) {
+            r = ddiv(a, dbl(fetch_s(vb, cb, lo >> 16)));
         } else if (cls == C_EXP) {
             r = StepMath<M>::exp(a);
         } else if (cls == C_LOG) {
             r = StepMath<M>::log(a);
-        } else if (cls == C_SQRT) {
-            r = StepMath<M>::sqrt(a);
         } else {
-            r = ddiv(a, b);
+            r = StepMath<M>::sqrt(a);
         }
-        V[(mw >> 48) & 0xfffu] = bits(r);
+        sts64(vb + (((hi >> 16) & 0xfffu) << 3), bits(r));
     }
-    if (mw >> 63) {
-        const uint64_t iw = e.y;
-        const uint32_t iop = static_cast<uint32_t>(iw >> 60);
-        const uint64_t A = fetch(V, C, static_cast<uint32_t>(iw) & 0xffffu);
-        const uint64_t B = fetch(V, C, static_cast<uint32_t>(iw >> 16) & 0xffffu);
-        const uint64_t Cc = fetch(V, C, static_cast<uint32_t>(iw >> 32) & 0xffffu);
-        uint64_t r = A;
-        r = iop == I_LE ? ble(A, B) : r;
-        r = iop == I_LT ? blt(A, B) : r;
-        r = iop == I_AND ? (A & B) : r;
-        r = iop == I_OR ? (A | B) : r;
-        r = iop == I_NOT ? (A ^ 1ULL) : r;
-        r = iop == I_SEL ? (A != 0 ? B : Cc) : r;
-        V[(iw >> 48) & 0xfffu] = r;
+    if (hi >> 31) {
+        const uint32_t ilo = static_cast<uint32_t>(e.y), ihi = static_cast<uint32_t>(e.y >> 32);
+        const uint64_t A = fetch_s(vb, cb, ilo & 0xffffu);
+        const uint64_t B = fetch_s(vb, cb, ilo >> 16);
+        const uint64_t Cc = fetch_s(vb, cb, ihi & 0xffffu);
+        uint64_t r = A != 0 ? B : Cc;
+        if (lo & 0x8000u) {  // the step carries comparisons (uniform over the warp)
+            const uint32_t iop = ihi >> 28;
+            r = iop == I_LE ? ble(A, B) : r;
+            r = iop == I_LT ? blt(A, B) : r;
+        }
+        sts64(vb + (((ihi >> 16) & 0xfffu) << 3), r);
     }
 }
 
 // One generated program on the group's cell: steps of (main word, integer word)
-// per lane; the group synchronises after every step.  Entries are loaded
-// kPrefetch steps ahead into a register ring.
-template <class M, int G, int NSTEPS>
-__device__ __forceinline__ void run_prog(const ulonglong2* __restrict__ prog, int gl, uint64_t* V, const uint64_t* C,
-                                         unsigned gmask) {
+// per lane; the group synchronises after every step.  One out-of-line copy serves
+// every call site (the instruction cache holds one loop), unrolled by four with the
+// next four steps' table entries loaded while the current four execute: the tables
+// (~100-200 KB per G) live mostly in L2, since shared memory takes most of L1.
+template <class M, int G>
+__device__ __noinline__ void run_prog(const ulonglong2* __restrict__ prog, int nsteps, int gl, uint64_t* V,
+                                      const uint64_t* C, unsigned gmask) {
+    const uint32_t vb = static_cast<uint32_t>(__cvta_generic_to_shared(V));
+    const uint32_t cb = static_cast<uint32_t>(__cvta_generic_to_shared(C));
     const ulonglong2* p = prog + gl;
-    ulonglong2 ring[kPrefetch];
-#pragma unroll
-    for (int j = 0; j < kPrefetch; ++j) ring[j] = j < NSTEPS ? __ldg(p + j * G) : make_ulonglong2(0, 0);
+    const ulonglong2 zero = make_ulonglong2(0, 0);
+    ulonglong2 e0 = nsteps > 0 ? __ldg(p) : zero;
+    ulonglong2 e1 = nsteps > 1 ? __ldg(p + G) : zero;
+    ulonglong2 e2 = nsteps > 2 ? __ldg(p + 2 * G) : zero;
+    ulonglong2 e3 = nsteps > 3 ? __ldg(p + 3 * G) : zero;
 #pragma unroll 1
-    for (int s0 = 0; s0 < NSTEPS; s0 += kPrefetch) {
-#pragma unroll
-        for (int j = 0; j < kPrefetch; ++j) {
-            const int s = s0 + j;
-            if (s < NSTEPS) {
-                const ulonglong2 e = ring[j];
-                if (s + kPrefetch < NSTEPS) ring[j] = __ldg(p + (s + kPrefetch) * G);
-                exec_step<M>(e, V, C);
-                __syncwarp(gmask);
-            }
+    for (int s = 0; s < nsteps; s += 4) {
+        const ulonglong2 n0 = s + 4 < nsteps ? __ldg(p + (s + 4) * G) : zero;
+        const ulonglong2 n1 = s + 5 < nsteps ? __ldg(p + (s + 5) * G) : zero;
+        const ulonglong2 n2 = s + 6 < nsteps ? __ldg(p + (s + 6) * G) : zero;
+        const ulonglong2 n3 = s + 7 < nsteps ? __ldg(p + (s + 7) * G) : zero;
+        exec_step<M>(e0, vb, cb);
+        group_sync(gmask);
+        if (s + 1 < nsteps) {
+            exec_step<M>(e1, vb, cb);
+            group_sync(gmask);
         }
+        if (s + 2 < nsteps) {
+            exec_step<M>(e2, vb, cb);
+            group_sync(gmask);
+        }
+        if (s + 3 < nsteps) {
+            exec_step<M>(e3, vb, cb);
+            group_sync(gmask);
+        }
+        e0 = n0;
+        e1 = n1;
+        e2 = n2;
+        e3 = n3;
     }
 }
 
@@ -423,7 +462,7 @@ __global__ void __launch_bounds__(W * 32, 1) k_advance_coop(DevState s, StepCtl*
         // ---- one ROS2S attempt, reproducer.cpp:7259-7345
         store_inputs<G, K>(V, y, gl);
         __syncwarp(gmask);
-        run_prog<M, G, Tab::kJSteps>(Tab::jprog(), gl, V, C, gmask);
+        run_prog<M, G>(Tab::jprog(), Tab::kJSteps, gl, V, C, gmask);
         load_outputs<G, K>(V, C, Tab::jout(), f0, gl);
         if (L.fresh) L.n_jac += 1;
         L.fresh = false;
@@ -474,7 +513,7 @@ __global__ void __launch_bounds__(W * 32, 1) k_advance_coop(DevState s, StepCtl*
             }
             store_inputs<G, K>(V, yn, gl);
             __syncwarp(gmask);
-            run_prog<M, G, Tab::kRSteps>(Tab::rprog(), gl, V, C, gmask);
+            run_prog<M, G>(Tab::rprog(), Tab::kRSteps, gl, V, C, gmask);
             double dy[K];
             load_outputs<G, K>(V, C, Tab::rout(), dy, gl);
 #pragma unroll
@@ -494,7 +533,7 @@ __global__ void __launch_bounds__(W * 32, 1) k_advance_coop(DevState s, StepCtl*
             __syncwarp(gmask);  // every lane has read the stage-2 outputs
             store_inputs<G, K>(V, yn, gl);
             __syncwarp(gmask);
-            run_prog<M, G, Tab::kRSteps>(Tab::rprog(), gl, V, C, gmask);
+            run_prog<M, G>(Tab::rprog(), Tab::kRSteps, gl, V, C, gmask);
             double dy[K];
             load_outputs<G, K>(V, C, Tab::rout(), dy, gl);
 #pragma unroll
@@ -597,7 +636,7 @@ __global__ void k_diag_coop_network(int n, const double* __restrict__ y, double*
     }
     store_inputs<G, K>(V, yy, gl);
     __syncwarp(gmask);
-    run_prog<M, G, Tab::kJSteps>(Tab::jprog(), gl, V, C, gmask);
+    run_prog<M, G>(Tab::jprog(), Tab::kJSteps, gl, V, C, gmask);
     load_outputs<G, K>(V, C, Tab::jout(), out, gl);
     for (int i = gl; i < NEQ * NEQ; i += G) J[static_cast<size_t>(cell) * NEQ * NEQ + i] = -E[i];
 #pragma unroll
@@ -608,7 +647,7 @@ __global__ void k_diag_coop_network(int n, const double* __restrict__ y, double*
     __syncwarp(gmask);
     store_inputs<G, K>(V, yy, gl);
     __syncwarp(gmask);
-    run_prog<M, G, Tab::kRSteps>(Tab::rprog(), gl, V, C, gmask);
+    run_prog<M, G>(Tab::rprog(), Tab::kRSteps, gl, V, C, gmask);
     load_outputs<G, K>(V, C, Tab::rout(), out, gl);
 #pragma unroll
     for (int t = 0; t < K; ++t) {

@@ -517,28 +517,30 @@ __device__ __forceinline__ void lu_solve_f32(MT LU, const uint64_t ip, float* x)
     }
 }
 
-// x <- E^-1 x with E = fac*I - J: FP32 solve, FP64 residual b - E x0 (J from the
-// lane's FP64 backup), FP32 correction
+// x <- E^-1 x with E = fac*I - J, the FP32 factors being those of W^-1 E W
+// (error-weighted variables, W = diag(atol + rtol |y|)): FP32 solve of
+// W^-1 E W x' = W^-1 b, x0 = W x', one FP64 residual r = b - E x0 (J from the
+// lane's FP64 backup), FP32 correction solve of the scaled residual
 template <class MT>
 __device__ __forceinline__ void solve_refined(MT LU, const uint64_t ip, const double* jb, int stride, double fac,
-                                              double* x) {
+                                              const double* w, double* x) {
     float xf[NEQ];
 #pragma unroll
-    for (int i = 0; i < NEQ; ++i) xf[i] = __double2float_rn(x[i]);
+    for (int i = 0; i < NEQ; ++i) xf[i] = __double2float_rn(ddiv(x[i], w[i]));
     lu_solve_f32(LU, ip, xf);
     double x0[NEQ];
 #pragma unroll
-    for (int i = 0; i < NEQ; ++i) x0[i] = static_cast<double>(xf[i]);
+    for (int i = 0; i < NEQ; ++i) x0[i] = static_cast<double>(xf[i]) * w[i];
 #pragma unroll
     for (int i = 0; i < NEQ; ++i) {
         double acc = 0.0;
 #pragma unroll
         for (int j = 0; j < NEQ; ++j) acc = acc + jb[(i * NEQ + j) * stride] * x0[j];
-        xf[i] = __double2float_rn(x[i] - (fac * x0[i] - acc));
+        xf[i] = __double2float_rn(ddiv(x[i] - (fac * x0[i] - acc), w[i]));
     }
     lu_solve_f32(LU, ip, xf);
 #pragma unroll
-    for (int i = 0; i < NEQ; ++i) x[i] = x0[i] + static_cast<double>(xf[i]);
+    for (int i = 0; i < NEQ; ++i) x[i] = x0[i] + static_cast<double>(xf[i]) * w[i];
 }
 
 struct Lane {
@@ -581,6 +583,7 @@ __global__ void __launch_bounds__(B, MINB) k_advance(DevState s, StepCtl* ctl, d
     bool alive = true;   // lane may still take cells
     bool have = false;   // lane holds a cell
     double y[NEQ], f0[NEQ];
+    double wsc[PREC ? NEQ : 1];  // precision form: the error weights of the attempt
     uint64_t ip = 0;
 
     while (__any_sync(0xffffffffu, alive)) {
@@ -726,13 +729,17 @@ __global__ void __launch_bounds__(B, MINB) k_advance(DevState s, StepCtl* ctl, d
                 for (int i = 0; i < NEQ; ++i) E(i, i) = E(i, i) + fac;
                 info = lu_decompose(E, ip);
             } else {
+                // error-weighted variables: the controller's own scale per component
+#pragma unroll
+                for (int i = 0; i < NEQ; ++i)
+                    wsc[i] = (i < NS ? kAtolSpec : kAtolEnergy) + (i < NS ? kRtolSpec : kRtolEnergy) * ::fabs(y[i]);
 #pragma unroll 1
                 for (int r = 0; r < NEQ; ++r)
 #pragma unroll
                     for (int c = 0; c < NEQ; ++c) {
                         double v = -jb[(r * NEQ + c) * nslots];
                         if (r == c) v = v + fac;
-                        E32(r, c) = __double2float_rn(v);
+                        E32(r, c) = __double2float_rn(ddiv(v * wsc[c], wsc[r]));
                     }
                 info = lu_decompose_f32(E32, ip);
             }
@@ -760,7 +767,7 @@ __global__ void __launch_bounds__(B, MINB) k_advance(DevState s, StepCtl* ctl, d
 #pragma unroll
                 for (int i = 0; i < NEQ; ++i) ak1[i] = f0[i];
                 if constexpr (PREC == 0) lu_solve(E, ip, ak1);
-                else solve_refined(E32, ip, jb, nslots, fac, ak1);
+                else solve_refined(E32, ip, jb, nslots, fac, wsc, ak1);
                 // stages 2 and 3 share one inlined RHS evaluation
 #pragma unroll 1
                 for (int stage = 2; stage <= 3; ++stage) {
@@ -784,7 +791,7 @@ __global__ void __launch_bounds__(B, MINB) k_advance(DevState s, StepCtl* ctl, d
 #pragma unroll
                     for (int i = 0; i < NEQ; ++i) w[i] += dy[i];
                     if constexpr (PREC == 0) lu_solve(E, ip, w);
-                    else solve_refined(E32, ip, jb, nslots, fac, w);
+                    else solve_refined(E32, ip, jb, nslots, fac, wsc, w);
                     if (stage == 2) {
 #pragma unroll
                         for (int i = 0; i < NEQ; ++i) ak2[i] = w[i];

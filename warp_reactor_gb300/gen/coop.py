@@ -11,11 +11,14 @@ synchronises, so a step may use any value produced by an earlier step.
 Step format (per lane, two 64-bit words):
 
 * main word: class (3 bits: none, fma, exp, log, sqrt, div), "has integer part"
-  (1 bit), destination slot (12 bits) and three operands (16 bits each);
-* integer word: op (copy, le, lt, and, or, not, sel), destination and three
-  operands.  Every step may carry up to ``G`` integer nodes beside its main node,
-  so comparisons, selects and boolean logic ride along with the floating-point
-  work instead of taking steps of their own.
+  (1 bit), destination slot (12 bits) and three operands (16 bits each; bit 15 of
+  the first says "the integer part holds comparisons");
+* integer word: op (select, le, lt), destination and three operands.  Every
+  step may carry up to ``G`` integer nodes beside its main node, so comparisons,
+  selects and boolean logic ride along with the floating-point work instead of
+  taking steps of their own.  Boolean logic and copies are selects A ? B : C with
+  the boolean constants as operands: a and b = a ? b : 0, a or b = a ? 1 : b,
+  not a = a ? 0 : 1, copy x = 1 ? x : 1.
 
 Operand: slot index (12 bits), "constant table" flag, negate flag and absolute
 value flag.  ``neg`` and ``abs`` nodes of the DAG are therefore never computed:
@@ -66,11 +69,13 @@ from . import ir_io
 # main classes
 C_NONE, C_FMA, C_EXP, C_LOG, C_SQRT, C_DIV = 0, 1, 2, 3, 4, 5
 # integer ops
-I_COPY, I_LE, I_LT, I_AND, I_OR, I_NOT, I_SEL = 0, 1, 2, 3, 4, 5, 6
+# integer ops: every copy / and / or / not / select is one select A ? B : C (with
+# boolean constants 0 and 1 as operands), comparisons are the other two
+I_SEL, I_LE, I_LT = 0, 1, 2
 
 MAIN_CLASS = {"add": C_FMA, "sub": C_FMA, "mul": C_FMA, "exp": C_EXP, "cexp": C_EXP, "log": C_LOG,
               "clog": C_LOG, "sqrt": C_SQRT, "csqrt": C_SQRT, "div": C_DIV}
-INT_OP = {"le": I_LE, "lt": I_LT, "and": I_AND, "or": I_OR, "not": I_NOT, "sel": I_SEL, "copy": I_COPY}
+INT_OP = {"le": I_LE, "lt": I_LT, "and": I_SEL, "or": I_SEL, "not": I_SEL, "sel": I_SEL, "copy": I_SEL}
 # FP64 issue slots of one step of each class (measured call throughput of CUDA's
 # exp/log/sqrt on GB300; division runs on the integer pipe)
 STEP_COST = {C_FMA: 1.0, C_EXP: 19.0, C_LOG: 29.0, C_SQRT: 9.0, C_DIV: 0.5}
@@ -84,6 +89,9 @@ MAX_SLOTS = 1 << SLOT_BITS
 OPF_CONST = 1 << 12
 OPF_NEG = 1 << 13
 OPF_ABS = 1 << 14
+# bit 15 of the main word (unused by its first operand): the step's integer part
+# holds comparisons, so only such steps run the comparison code
+OPF_STEP_CMP = 1 << 15
 
 FLOOR = 1.0e-100  # reproducer.cpp:231
 # species masses, reproducer.cpp:233-248 (the literals of wr_physics.cuh)
@@ -328,6 +336,9 @@ def schedule(P: Program, out: dict, G: int, copy_jac: bool, reverse: bool = Fals
 def encode(P: Program, sch: Schedule, args, cidx: dict, sink: int, one: int, mzero: int):
     """Per-step, per-lane (main, int) words."""
     G = sch.G
+    # boolean constants (the integers 0 and 1)
+    c_true = cidx[1] | OPF_CONST
+    c_false = cidx[0] | OPF_CONST
 
     def operand(x, neg=False, ab=False):
         b, n2, a2 = resolve(P, x)
@@ -366,22 +377,27 @@ def encode(P: Program, sch: Schedule, args, cidx: dict, sink: int, one: int, mze
                 p = q = s = c_one
                 dst = sink
             hi = (cls << 60) | ((1 << 63) if riders else 0)
-            main = hi | (dst << 48) | (s << 32) | (q << 16) | p
+            has_cmp = any(P.nodes[x][0] in ("le", "lt") for x in riders)
+            main = hi | (dst << 48) | (s << 32) | (q << 16) | p | (OPF_STEP_CMP if has_cmp else 0)
             if g < len(riders):
                 x = riders[g]
                 op, a = P.nodes[x]
                 iop = INT_OP[op]
                 if op == "copy":  # E = -J
-                    ops = [operand(a[0], neg=True), c_one, c_one]
+                    ops = [c_true, operand(a[0], neg=True), c_true]
+                elif op == "and":
+                    ops = [operand(a[0]), operand(a[1]), c_false]
+                elif op == "or":
+                    ops = [operand(a[0]), c_true, operand(a[1])]
                 elif op == "not":
-                    ops = [operand(a[0]), c_one, c_one]
+                    ops = [operand(a[0]), c_false, c_true]
                 elif op == "sel":
                     ops = [operand(a[0]), operand(a[1]), operand(a[2])]
-                else:
-                    ops = [operand(a[0]), operand(a[1]), c_one]
+                else:  # le, lt
+                    ops = [operand(a[0]), operand(a[1]), c_true]
                 idst = sch.slot[x]
             else:
-                iop, ops, idst = I_COPY, [c_one, c_one, c_one], sink
+                iop, ops, idst = I_SEL, [c_true, c_one, c_one], sink
             iw = (iop << 60) | (idst << 48) | (ops[2] << 32) | (ops[1] << 16) | ops[0]
             lanes.append((main, iw))
         words.append(lanes)
@@ -403,7 +419,7 @@ def generate(G: int, dag=None):
             if P.nodes[x][0] == "const":
                 consts.add(P.nodes[x][1][0])
     one, mzero = dbits(1.0), dbits(-0.0)
-    consts |= {one, mzero}
+    consts |= {one, mzero, 0, 1}
     ctab = sorted(consts)
     cidx = {b: i for i, b in enumerate(ctab)}
     if len(ctab) > MAX_SLOTS:
