@@ -36,7 +36,7 @@ def _parse(stdout):
 
 @pytest.mark.gpu
 def test_grid1_prints_state(exe, gpu, oracle_port):
-    r = run(exe, "--grid", "1")
+    r = run(exe, "--grid", "1", "--math", "portable")
     assert r.returncode == 0, r.stderr
     v = _parse(r.stdout)
     assert v["driver policy"] == "gridwide-independent"
@@ -50,7 +50,7 @@ def test_grid1_prints_state(exe, gpu, oracle_port):
 
 @pytest.mark.gpu
 def test_grid2_file_rotation_and_compare(exe, gpu, tmp_path, oracle_port, wr):
-    r = run(exe, "--grid", "2", cwd=tmp_path)
+    r = run(exe, "--grid", "2", "--math", "portable", cwd=tmp_path)
     assert r.returncode == 0, r.stderr
     f = tmp_path / "final_states_grid2_cuda.bin"
     assert f.stat().st_size == 8 * 172
@@ -59,7 +59,7 @@ def test_grid2_file_rotation_and_compare(exe, gpu, tmp_path, oracle_port, wr):
     oracle_port.run(cells, perturb=True)
     assert got.tobytes() == wr.pack_final_states(cells, 2).tobytes()
     # second run rotates the file and compares against the first: PASS, exit 0
-    r = run(exe, "--grid", "2", "--compare-final-state", str(f), cwd=tmp_path)
+    r = run(exe, "--grid", "2", "--math", "portable", "--compare-final-state", str(f), cwd=tmp_path)
     assert r.returncode == 0 and r.stdout.rstrip().endswith("PASS"), r.stdout
     assert "existing final states moved to:" in r.stdout
     assert len(list(tmp_path.glob("final_states_grid2_cuda.bin.old.*"))) == 1
@@ -69,7 +69,7 @@ def test_grid2_file_rotation_and_compare(exe, gpu, tmp_path, oracle_port, wr):
     bad["completed_steps"][5] += 1
     badf = tmp_path / "bad.bin"
     bad.tofile(badf)
-    r = run(exe, "--grid", "2", f"--compare-final-state={badf}", cwd=tmp_path)
+    r = run(exe, "--grid", "2", "--math", "portable", f"--compare-final-state={badf}", cwd=tmp_path)
     assert r.returncode == 1 and r.stdout.rstrip().endswith("FAIL")
     assert "first comparison failure: metadata mismatch at cell 3" not in r.stdout
     csv = (tmp_path / "final_state_comparison_failures_cuda.csv").read_text().splitlines()
@@ -79,6 +79,18 @@ def test_grid2_file_rotation_and_compare(exe, gpu, tmp_path, oracle_port, wr):
     # wrong-size file: read error, FAIL
     r = run(exe, "--grid", "2", "--compare-final-state", str(tmp_path / "missing.bin"), cwd=tmp_path)
     assert r.returncode == 1 and "failed to open final-state comparison file" in r.stderr
+
+
+@pytest.mark.gpu
+def test_default_math_equals_reference_cuda_kernel(exe, gpu, tmp_path, wr):
+    """With no --math the program computes in CUDA math and writes the final
+    states of the reference's own CUDA build (reproducer.cpp compiled with nvcc
+    for sm_103a, run on GB300) byte for byte, and the comparator passes on them."""
+    ref = os.path.join(os.path.dirname(__file__), "golden", "refcuda_grid4.bin")
+    r = run(exe, "--grid", "4", "--compare-final-state", ref, cwd=tmp_path)
+    assert r.returncode == 0 and r.stdout.rstrip().endswith("PASS"), r.stdout
+    got = (tmp_path / "final_states_grid4_cuda.bin").read_bytes()
+    assert got == open(ref, "rb").read()
 
 
 def test_policy_and_write_flags_parse(exe):
@@ -92,7 +104,8 @@ def test_policy_and_write_flags_parse(exe):
 @pytest.mark.gpu
 def test_legacy_local_cli_and_manifest(exe, gpu, tmp_path, oracle_port, wr):
     out = tmp_path / "legacy.bin"
-    r = run(exe, "--grid", "2", "--driver-policy", "legacy-local", "--write-final-state", str(out), cwd=tmp_path)
+    r = run(exe, "--grid", "2", "--math", "portable", "--driver-policy", "legacy-local",
+            "--write-final-state", str(out), cwd=tmp_path)
     assert r.returncode == 0, r.stderr
     assert "driver policy: legacy-local" in r.stdout
     cells = oracle_port.make_grid(2)
@@ -109,7 +122,8 @@ def test_cta32_cli(exe, gpu, tmp_path, oracle_port, wr):
     """--driver-policy gridwide-cta32 prints the reference structured build's policy
     name and writes the tile-controller final states."""
     out = tmp_path / "cta32.bin"
-    r = run(exe, "--grid", "2", "--driver-policy", "gridwide-cta32", "--write-final-state", str(out), cwd=tmp_path)
+    r = run(exe, "--grid", "2", "--math", "portable", "--driver-policy", "gridwide-cta32",
+            "--write-final-state", str(out), cwd=tmp_path)
     assert r.returncode == 0, r.stderr
     assert "driver policy: gridwide-structured-cta32" in r.stdout
     cells = oracle_port.make_grid(2)

@@ -3,10 +3,13 @@
 ``gen/coop.py`` turns the network DAG (with the burn_state_from_y prologue) into
 steps of G lanes.  This test executes those steps exactly as the device does --
 every lane gathers its operands, then every lane stores its result, one step at a
-time -- with the oracle's own exp/log, and requires the Jacobian (written into the
-matrix slots as E = -J) and the RHS to equal the oracle's jacobian(y) / rhs(y)
-bit for bit.  It also checks the schedule's hazards: no lane reads a slot that
-another lane writes in the same step.
+time -- with the oracle's own exp/log, then gathers E = -J into the matrix slots
+from the Jacobian output table, and requires the Jacobian and the RHS to equal the
+oracle's jacobian(y) / rhs(y) bit for bit.  It also checks the schedule's hazards
+(no lane reads a slot that another lane writes in the same step) and the slot
+map: the RHS-only program leaves the matrix slots (the LU factors) alone, and the
+Jacobian program's kept values lie above them, so the gather reads no slot it
+writes.
 """
 import math
 import struct
@@ -48,7 +51,7 @@ def fma_special(a, b, c, one, mzero):
     return a + c
 
 
-def run(words, V, C, oracle, one, mzero):
+def run(words, V, C, oracle, one, mzero, written=None):
     for lanes in words:
         reads, writes, results = set(), set(), []
         for mw, iw in lanes:
@@ -82,6 +85,8 @@ def run(words, V, C, oracle, one, mzero):
             assert dst == sink or dst not in reads, f"slot {dst} written and read in one step"
             assert dst == sink or dst not in writes, f"slot {dst} written twice in one step"
             writes.add(dst)
+            if written is not None and dst != len(V) - 1:
+                written.add(dst)
             V[dst] = r
 
 
@@ -122,12 +127,21 @@ def test_programs_equal_oracle(programs, oracle_port, G):
             V = [0] * gen["nv"]
             for k in range(15):
                 V[coop.Y_BASE + k] = u(y[k])
-            run(pr["words"], V, C, oracle_port, one, mzero)
+            written = set()
+            run(pr["words"], V, C, oracle_port, one, mzero, written)
             f = np.array([d(fetch(V, C, o)) for o in pr["rhs_out"]])
             assert same(f, f_o), (G, kind)
+            assert all(o & 0x1000 or (o & 0xfff) >= coop.E_SLOTS for o in pr["rhs_out"])
             if kind == "jrhs":
+                jac = pr["jac_out"]
+                assert len(jac) == 225
+                assert all(o & 0x1000 or (o & 0xfff) >= coop.E_SLOTS for o in jac)
+                for i in range(225):  # the kernel's gather: E = -J
+                    V[i] = fetch(V, C, jac[i])
                 J = -np.array([d(V[i]) for i in range(225)]).reshape(15, 15)
                 assert same(J, J_o), G
+            else:
+                assert not any(w < coop.E_SLOTS for w in written), "RHS program writes a matrix slot"
 
 
 @pytest.mark.parametrize("G", [8, 16, 32])
@@ -136,6 +150,8 @@ def test_program_shape(programs, G):
     main word names one class for all lanes."""
     gen = programs[G]
     assert gen["nv"] <= 4096 and len(gen["consts"]) <= 4096
+    ncpad = (len(gen["consts"]) + 1) & ~1
+    assert (ncpad + gen["warps"] * (32 // G) * gen["nv"]) * 8 <= coop.SMEM_BLOCK
     for pr in gen["progs"].values():
         for lanes in pr["words"]:
             assert len({(mw >> 60) for mw, _ in lanes}) == 1

@@ -81,7 +81,7 @@ def test_batching_workload_replay(wr, gpu, oracle_port):
     with wr.Context(grids=sizes, math=wr.MATH_PORTABLE) as ctx:
         ctx.upload(cells)
         best = ctx.autotune(True, steps=3)
-        assert best in (0, 1, 2, 4)
+        assert best in (0, 1, 2, 4, 5, 6, 7)  # an exact shape, never the precision form
         rc, _ = ctx.run(True)
         results = [ctx.grid_result(g) for g in range(len(sizes))]
         hists = [ctx.dt_history(g) for g in range(len(sizes))]

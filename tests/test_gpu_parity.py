@@ -390,7 +390,7 @@ def test_cta32_policy_equals_reference_structured_kernel(wr, gpu, grid):
     assert wr.pack_final_states(cells, grid).tobytes() == ref.tobytes()
 
 
-@pytest.mark.parametrize("grid", [2, 3, 4, 5])
+@pytest.mark.parametrize("grid", [3, 4])  # a partial tile of 27 cells; two full tiles
 def test_cta32_policy_bitwise(wr, gpu, oracle_port, grid):
     """WR_POLICY_GRIDWIDE_CTA32 (one controller per 32-cell tile, the reference's
     structured CUDA policy) on the GPU equals the oracle's restatement bit for bit;

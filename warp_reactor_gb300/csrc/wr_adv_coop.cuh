@@ -1,8 +1,8 @@
 // wr_adv_coop.cuh -- one translation unit per lanes-per-cell count G: the
 // generated vector programs of that G (coop_prog_g<G>.h, large initialisers) and
 // the cooperative advance kernel instantiated for both math policies.  The unit
-// defines WR_COOP_G and WR_COOP_W (warps per block: as many as the block's shared
-// memory holds) and includes generated/coop_prog_g<G>.h before this file.
+// defines WR_COOP_G and includes generated/coop_prog_g<G>.h (which sets the warps
+// per block: as many as the block's shared memory holds) before this file.
 #include "wr_launch.h"
 #include "wr_coop.cuh"
 
@@ -23,12 +23,13 @@ struct Tab {
     static __device__ __forceinline__ const ulonglong2* jprog() { return cp::kJRHSProg; }
     static __device__ __forceinline__ const ulonglong2* rprog() { return cp::kRHSProg; }
     static __device__ __forceinline__ const uint16_t* jout() { return cp::kJRHSOut; }
+    static __device__ __forceinline__ const uint16_t* jac() { return cp::kJRHSJac; }
     static __device__ __forceinline__ const uint16_t* rout() { return cp::kRHSOut; }
     static __device__ __forceinline__ const uint64_t* cst() { return cp::kConst; }
 };
 
 constexpr int kG = WR_COOP_G;
-constexpr int kW = WR_COOP_W;
+constexpr int kW = cp::kWarps;
 constexpr size_t kSmem = (static_cast<size_t>(Tab::kNCPad) + static_cast<size_t>(kW) * (32 / kG) * Tab::kNV) * 8;
 static_assert(kSmem <= 232448, "cooperative advance: shared memory of one block exceeds 227 KiB");
 }  // namespace

@@ -344,10 +344,22 @@ __device__ __forceinline__ void load_outputs(const uint64_t* V, const uint64_t* 
     }
 }
 
+// E = -J into the matrix slots after the Jacobian program.  The program uses the
+// matrix slots as scratch and keeps its results (the Jacobian entries and the
+// RHS) above them; the generated table names, per matrix entry r * 15 + c, the
+// slot or constant that holds J(r, c) with the negation as an operand modifier.
+template <int G>
+__device__ __forceinline__ void gather_matrix(uint64_t* V, const uint64_t* C, const uint16_t* jac, int gl,
+                                              unsigned gmask) {
+#pragma unroll 1
+    for (int i = gl; i < NEQ * NEQ; i += G) V[kE + i] = fetch(V, C, jac[i]);
+    __syncwarp(gmask);
+}
+
 // Generated tables of one G, supplied by the translation unit that includes the
 // generated header (one unit per G keeps the large initialisers apart).
 //   Tab::kNV, Tab::kNC, Tab::kJSteps, Tab::kRSteps and device accessors
-//   jprog(), rprog(), jout(), rout(), cst().
+//   jprog(), rprog(), jout(), jac(), rout(), cst().
 
 }  // namespace coop
 
@@ -464,6 +476,7 @@ __global__ void __launch_bounds__(W * 32, 1) k_advance_coop(DevState s, StepCtl*
         __syncwarp(gmask);
         run_prog<M, G>(Tab::jprog(), Tab::kJSteps, gl, V, C, gmask);
         load_outputs<G, K>(V, C, Tab::jout(), f0, gl);
+        gather_matrix<G>(V, C, Tab::jac(), gl, gmask);
         if (L.fresh) L.n_jac += 1;
         L.fresh = false;
         const double h = L.h;
@@ -638,6 +651,7 @@ __global__ void k_diag_coop_network(int n, const double* __restrict__ y, double*
     __syncwarp(gmask);
     run_prog<M, G>(Tab::jprog(), Tab::kJSteps, gl, V, C, gmask);
     load_outputs<G, K>(V, C, Tab::jout(), out, gl);
+    gather_matrix<G>(V, C, Tab::jac(), gl, gmask);
     for (int i = gl; i < NEQ * NEQ; i += G) J[static_cast<size_t>(cell) * NEQ * NEQ + i] = -E[i];
 #pragma unroll
     for (int t = 0; t < K; ++t) {

@@ -19,14 +19,16 @@ constexpr int kPrepareThreads = 256;
 //      memory (900 B per lane) with one FP64 residual refinement per stage solve
 //   4  384 threads x 1 block per SM (at most 168 registers per thread: more spills,
 //      twelve warps per SM to hide them)
-//   5  cooperative advance (wr_coop.cuh), 8 lanes per cell, 6 warps per SM
-//   6  cooperative advance, 16 lanes per cell, 12 warps per SM
-//   7  cooperative advance, 32 lanes per cell, 16 warps per SM
+//   5  cooperative advance (wr_coop.cuh), 8 lanes per cell
+//   6  cooperative advance, 16 lanes per cell
+//   7  cooperative advance, 32 lanes per cell
+//   (cooperative advance: one block per SM, as many warps as the cells' slot
+//   arrays fit in its shared memory, kWarps of generated/coop_prog_g<G>.h)
 constexpr int kAdvanceVariants = 8;
 constexpr int kPrecisionVariant = 3;
 constexpr int kDefaultVariant = 6;
 struct AdvanceShape {
-    int threads;
+    int threads;    // lane-per-cell shapes (0 for the cooperative advance)
     int blocks_per_sm;
     bool smem_matrix;
     int precision;  // 0 FP64 factorisation, 1 FP32 factorisation + FP64 refinement
@@ -34,7 +36,7 @@ struct AdvanceShape {
 };
 constexpr AdvanceShape kAdvanceShapes[kAdvanceVariants] = {
     {128, 1, true, 0, 0},  {128, 2, false, 0, 0}, {256, 1, false, 0, 0},  {256, 1, true, 1, 0},
-    {384, 1, false, 0, 0}, {192, 1, false, 0, 8}, {384, 1, false, 0, 16}, {512, 1, false, 0, 32}};
+    {384, 1, false, 0, 0}, {0, 1, false, 0, 8}, {0, 1, false, 0, 16}, {0, 1, false, 0, 32}};
 constexpr bool is_coop(int variant) { return kAdvanceShapes[variant].coop_lanes != 0; }
 
 constexpr size_t advance_smem_bytes(int variant) {

@@ -21,7 +21,7 @@ import ctypes
 
 import numpy as np
 
-from . import COLLAPSE_STATE, MAX_COLLAPSE_STEPS, SUCCESS, Context, WarpReactorError, lib
+from . import COLLAPSE_STATE, MATH_PORTABLE, MAX_COLLAPSE_STEPS, SUCCESS, Context, WarpReactorError, lib
 
 _declared = False
 
@@ -51,8 +51,9 @@ def num_multipliers() -> int:
 
 def schedule(cells: np.ndarray, perturb: bool = True, device: int = 0) -> np.ndarray:
     """Outer schedule of a plain gridwide run of ``cells``: the grid timestep of
-    every outer step (wr_grid_dt_history), trimmed to the steps taken."""
-    with Context(len(cells), device=device) as ctx:
+    every outer step (wr_grid_dt_history), trimmed to the steps taken.  The run
+    uses the portable math, the arithmetic of the differentiation map."""
+    with Context(len(cells), device=device, math=MATH_PORTABLE) as ctx:
         ctx.upload(np.ascontiguousarray(cells))
         rc, _ = ctx.run(perturb)
         if rc != SUCCESS:

@@ -42,21 +42,26 @@ Two programs are generated per ``G``:
 * ``jrhs``: inputs ``y[0..14]`` (the ROS2S state: 14 number densities and the
   internal energy); prologue ``burn_state_from_y`` (reproducer.cpp:7029-7038):
   ``X = max(y, 1e-100)`` and ``T = eos_re(X, e)`` (reproducer.cpp:284-314);
-  then the fused analytic Jacobian + RHS of ``network.ir``.  The Jacobian is
-  written straight into the cell's iteration matrix as ``E = -J`` (slots
-  ``r*15 + c``), the RHS values stay in slots listed in the program's output
-  table;
+  then the fused analytic Jacobian + RHS of ``network.ir``.  The Jacobian's 225
+  entries and the RHS are kept values; after the program the kernel gathers
+  ``E = -J`` into the matrix slots through the program's Jacobian table (one
+  operand per entry ``r*15 + c``, the negation as a modifier);
 * ``rhs``: the same prologue and the RHS only.
 
-Slot map of a cell: ``[0, 225)`` the iteration matrix (never used as scratch, so
-the LU factors survive the stage RHS evaluations), ``[225, 240)`` the inputs, then
-scratch values allocated by a linear scan over the schedule; the last slot is a
-write sink for idle lanes.
+Slot map of a cell: ``[0, 225)`` the iteration matrix, ``[225, 240)`` the
+inputs, then scratch; the last slot is a write sink for idle lanes.  The Jacobian
+program runs before the matrix is formed, so it uses the matrix slots as scratch
+too and keeps its results above them; the RHS program runs while the matrix holds
+the LU factors and never writes it.  Slots are allocated by a linear scan over
+the schedule, so the slot count is the largest live set, which sets the shared
+memory per cell and hence the cells (warps) per SM.
 
 Scheduling is list scheduling by critical path (longest weighted path to an
-output) with one class per step.  Every schedule of the DAG gives the same bits:
-each node is the same operation on the same operands wherever and whenever it is
-computed.
+output) with one class per step; above a live-set limit, nodes whose operands die
+with them go first; integer nodes then move as late as their users allow.
+Long chains of boolean logic are rebalanced first (``rebalance_boolean_chains``).
+Every schedule of the DAG gives the same bits: each node is the same operation on
+the same operands wherever and whenever it is computed.
 """
 from __future__ import annotations
 
@@ -75,7 +80,7 @@ I_SEL, I_LE, I_LT = 0, 1, 2
 
 MAIN_CLASS = {"add": C_FMA, "sub": C_FMA, "mul": C_FMA, "exp": C_EXP, "cexp": C_EXP, "log": C_LOG,
               "clog": C_LOG, "sqrt": C_SQRT, "csqrt": C_SQRT, "div": C_DIV}
-INT_OP = {"le": I_LE, "lt": I_LT, "and": I_SEL, "or": I_SEL, "not": I_SEL, "sel": I_SEL, "copy": I_SEL}
+INT_OP = {"le": I_LE, "lt": I_LT, "and": I_SEL, "or": I_SEL, "not": I_SEL, "sel": I_SEL}
 # FP64 issue slots of one step of each class (measured call throughput of CUDA's
 # exp/log/sqrt on GB300; division runs on the integer pipe)
 STEP_COST = {C_FMA: 1.0, C_EXP: 19.0, C_LOG: 29.0, C_SQRT: 9.0, C_DIV: 0.5}
@@ -170,7 +175,88 @@ def build(dag, kind: str) -> tuple:
     out = {"rhs": [m[dag.outputs[("rhs", i)]] for i in range(15)]}
     if kind == "jrhs":
         out["jac"] = {(r, c): m[dag.outputs[("jac", r, c)]] for r in range(15) for c in range(15)}
+    rebalance_boolean_chains(P)
     return P, out
+
+
+BOOL_OPS = ("and", "or", "not")
+
+
+def rebalance_boolean_chains(P: Program, min_depth: int = 12):
+    """Shorten long chains of boolean logic.
+
+    The network holds conditions folded over many terms, c_k+1 = or(a_k,
+    and(c_k, not(b_k))), ~150 levels deep: evaluated as written they need one
+    step each at the end of the RHS program.  Along such a chain (each link
+    the only user of the one below) every link is a map of the chain value c in
+    {0, 1}: and(c, s) -> (0, s), or(c, s) -> (s, 1), not(c) -> (1, 0), written
+    as the pair (value at c = 0, value at c = 1).  Maps compose exactly,
+    (g o f)(i) = f(i) ? g(1) : g(0), so a balanced tree of compositions gives the
+    whole chain's map in log2(length) levels of selects, and the top node
+    becomes sel(c_0, map(1), map(0)).  Booleans are the integers 0 and 1, so
+    the value of every node is unchanged."""
+    zero, one = P.const_bits(0), P.const_bits(1)
+    memo = {}
+
+    def sel(c, a, b):
+        if c == one:
+            return a
+        if c == zero or a == b:
+            return b
+        if a == one and b == zero:
+            return c
+        key = ("sel", c, a, b)
+        if key not in memo:
+            memo[key] = P.add("sel", c, a, b)
+        return memo[key]
+
+    def compose(g, f):  # g after f
+        return sel(f[0], g[1], g[0]), sel(f[1], g[1], g[0])
+
+    while True:
+        users = collections.defaultdict(list)
+        depth = {}
+        for i, (op, a) in enumerate(P.nodes):
+            if op in ("in", "const"):
+                continue
+            for y in a:
+                users[y].append(i)
+            if op in BOOL_OPS:
+                depth[i] = 1 + max((depth.get(y, 0) for y in a), default=0)
+        if not depth:
+            return
+        top = max(depth, key=lambda x: (depth[x], -x))
+        if depth[top] < min_depth:
+            return
+        # the chain below top: follow the deepest boolean operand while it has
+        # no other user
+        links = []  # (node, chain operand) from the top down
+        x = top
+        while P.nodes[x][0] in BOOL_OPS:
+            op, a = P.nodes[x]
+            below = max(a, key=lambda y: depth.get(y, 0))
+            links.append((x, below))
+            if depth.get(below, 0) == 0 or len(users[below]) != 1 or P.nodes[below][0] not in BOOL_OPS:
+                break
+            x = below
+        if len(links) < min_depth:
+            return
+        maps = []  # bottom-up link maps
+        for x, below in reversed(links):
+            op, a = P.nodes[x]
+            if op == "not":
+                maps.append((one, zero))
+            else:
+                other = a[1] if a[0] == below else a[0]
+                maps.append((zero, other) if op == "and" else (other, one))
+        while len(maps) > 1:
+            nxt = [compose(maps[i + 1], maps[i]) for i in range(0, len(maps) - 1, 2)]
+            if len(maps) % 2:
+                nxt.append(maps[-1])
+            maps = nxt
+        m0, m1 = maps[0]
+        c0 = links[-1][1]
+        P.nodes[top] = ("sel", (c0, m1, m0))
 
 
 def resolve(P: Program, x: int):
@@ -198,20 +284,34 @@ class Schedule:
         self.consts = consts
 
 
-def list_schedule(comp, args, users, kind, prio, G):
+def list_schedule(comp, args, users, kind, prio, G, limit=None):
     """Steps of width G: each step takes up to G ready nodes of one main class
     (highest priority first; a full step is preferred) and up to G ready integer
-    nodes.  ``args``/``users`` give the dependences in the direction scheduled."""
+    nodes.  ``args``/``users`` give the dependences in the direction scheduled.
+
+    ``limit``: once that many computed values are live (computed, with users not
+    yet scheduled), ready nodes are taken by their effect on the live set first
+    (a node whose operands die with it before one that only adds a value), then
+    by priority: the cell's shared memory is set by the largest live set."""
     pend = {x: len(set(args[x])) for x in comp}
+    remaining = {x: len(set(users[x])) for x in comp}
     ready = collections.defaultdict(list)
     for x in comp:
         if pend[x] == 0:
             ready[kind(x)].append(x)
     steps = []
     left = len(comp)
+    live = 0
     mains = (C_FMA, C_EXP, C_LOG, C_SQRT, C_DIV)
+
+    def key(x):
+        if limit is not None and live >= limit:
+            freed = sum(1 for a in set(args[x]) if remaining[a] == 1)
+            return ((1 if users[x] else 0) - freed, -prio[x])
+        return (0, -prio[x])
+
     while left:
-        rl = sorted(ready["int"], key=lambda x: -prio[x])
+        rl = sorted(ready["int"], key=key)
         riders, ready["int"] = rl[:G], rl[G:]
         cand = [c for c in mains if ready[c]]
         cls, take = C_NONE, []
@@ -219,11 +319,15 @@ def list_schedule(comp, args, users, kind, prio, G):
             full = [c for c in cand if len(ready[c]) >= G]
             pool = full if full else cand
             cls = max(pool, key=lambda c: (max(prio[x] for x in ready[c]), len(ready[c])))
-            rl = sorted(ready[cls], key=lambda x: -prio[x])
+            rl = sorted(ready[cls], key=key)
             take, ready[cls] = rl[:G], rl[G:]
         steps.append((cls, take, riders))
         left -= len(take) + len(riders)
         for x in take + riders:
+            live += 1 if users[x] else 0
+            for a in set(args[x]):
+                remaining[a] -= 1
+                live -= 1 if remaining[a] == 0 else 0
             for u in users[x]:
                 pend[u] -= 1
                 if pend[u] == 0:
@@ -231,21 +335,39 @@ def list_schedule(comp, args, users, kind, prio, G):
     return steps
 
 
-def schedule(P: Program, out: dict, G: int, copy_jac: bool, reverse: bool = False):
+def sink_riders(steps, users, kind, G):
+    """Move every integer node with users to the latest step before its first
+    user that has a free integer lane (integer nodes cost no FP64 issue slot, so
+    computing them late only shortens their values' lives); steps left empty are
+    dropped."""
+    done = {}
+    for s, (_, take, riders) in enumerate(steps):
+        for x in take + riders:
+            done[x] = s
+    lanes = [list(r) for _, _, r in steps]
+    for x in sorted((x for x in done if kind(x) == "int" and users[x]), key=lambda x: -done[x]):
+        first_use = min(done[u] for u in users[x])
+        for s in range(first_use - 1, done[x], -1):
+            if len(lanes[s]) < G:
+                lanes[done[x]].remove(x)
+                lanes[s].append(x)
+                done[x] = s
+                break
+    return [(cls, take, lanes[s]) for s, (cls, take, _) in enumerate(steps) if take or lanes[s]]
+
+
+def schedule(P: Program, out: dict, G: int, jac: bool, limit=None):
     """List-schedule the program into steps of width G and allocate slots.
 
-    ``reverse``: schedule from the outputs back to the inputs (each node as late
-    as its users allow, by depth from the inputs) and reverse the step list.
-    Values are then computed shortly before they are used, which keeps the live
-    set (the shared memory per cell) small at the same step count; forward
-    scheduling by critical path computes values as early as possible."""
+    ``jac``: the program computes the Jacobian too.  Its 225 entries are kept
+    values like the RHS (no matrix slot is reserved while the program runs, so
+    the iteration matrix's slots serve as scratch); after the program the kernel
+    gathers E = -J into the matrix slots from the ``jac`` output table.  Kept
+    values therefore live above the matrix slots.  The RHS-only program runs
+    while the matrix holds LU factors, so it never writes the matrix slots."""
     leaf = ("in", "const")
-    # pseudo nodes: E(r,c) = -J(r,c) copies into the matrix slots
-    copies = []
-    if copy_jac:
-        for (r, c), x in sorted(out["jac"].items()):
-            copies.append((P.add("copy", x), r * 15 + c))
-    roots = list(out["rhs"]) + [cp for cp, _ in copies]
+    jac_roots = [x for _, x in sorted(out["jac"].items())] if jac else []
+    roots = list(out["rhs"]) + jac_roots
     # live compute nodes (neg/abs folded)
     seen, stack = set(), [resolve(P, r)[0] for r in roots]
     while stack:
@@ -269,56 +391,59 @@ def schedule(P: Program, out: dict, G: int, copy_jac: bool, reverse: bool = Fals
     def kind(x):
         return MAIN_CLASS.get(P.nodes[x][0], "int")
 
-    if reverse:
-        depth = {}
-        for x in comp:
-            depth[x] = LATENCY[kind(x)] + max((depth[a] for a in cargs[x]), default=0.0)
-        rsteps = list_schedule(comp, {x: users[x] for x in comp}, cargs, kind, depth, G)
-        steps = rsteps[::-1]
-    else:
-        prio = {}
-        for x in reversed(comp):
-            prio[x] = LATENCY[kind(x)] + max((prio[u] for u in users[x]), default=0.0)
-        steps = list_schedule(comp, cargs, users, kind, prio, G)
+    # topological order (node indices are not one: rewrites add operands late)
+    pend = {x: len(cargs[x]) for x in comp}
+    order = [x for x in comp if pend[x] == 0]
+    for x in order:
+        for u in users[x]:
+            pend[u] -= 1
+            if pend[u] == 0:
+                order.append(u)
+    assert len(order) == len(comp), "the program has a cycle"
+    prio = {}
+    for x in reversed(order):
+        prio[x] = LATENCY[kind(x)] + max((prio[u] for u in users[x]), default=0.0)
+    steps = sink_riders(list_schedule(comp, cargs, users, kind, prio, G, limit), users, kind, G)
     done_at = {}
     for s, (cls, take, riders) in enumerate(steps):
         for x in take + riders:
             done_at[x] = s
     for x in comp:
         assert all(done_at[a] < done_at[x] for a in cargs[x]), "schedule violates a dependence"
-    # ---- slot allocation (linear scan; a slot read last in step s is free from s+1)
+    # ---- slot allocation (linear scan; a slot read last in step s is free from
+    # s+1).  Two pools: the matrix slots (scratch of the Jacobian program only)
+    # and the slots above the inputs; kept values come from the upper pool.
+    import heapq
     last = {}
     for s, (cls, take, riders) in enumerate(steps):
         for x in take + riders:
             for a in args[x]:
                 if P.nodes[a][0] == "in" or P.nodes[a][0] not in leaf:
                     last[a] = s
-    end = len(steps)
-    keep = {resolve(P, r)[0] for r in out["rhs"]}
+    keep = {resolve(P, r)[0] for r in roots}
     slot = {}
     inputs = [x for x in range(len(P.nodes)) if P.nodes[x][0] == "in"]
-    for x in inputs:
-        slot[x] = Y_BASE + P.nodes[x][1][0]
-    copy_dst = dict(copies)
-    free = []  # min-heap of free scratch slots
-    import heapq
+    low = list(range(E_SLOTS)) if jac else []  # min-heaps of free slots
+    high = []
     next_slot = Y_BASE + 15
     release = collections.defaultdict(list)
     for x in inputs:
+        slot[x] = Y_BASE + P.nodes[x][1][0]
+        if x in keep:
+            continue
         if x in last:
             release[last[x] + 1].append(slot[x])
         else:
-            heapq.heappush(free, slot[x])
+            heapq.heappush(high, slot[x])
     nv = next_slot
     for s, (cls, take, riders) in enumerate(steps):
         for sl in release.pop(s, []):
-            heapq.heappush(free, sl)
+            heapq.heappush(low if sl < E_SLOTS else high, sl)
         for x in take + riders:
-            if x in copy_dst:
-                slot[x] = copy_dst[x]
-                continue
-            if free:
-                sl = heapq.heappop(free)
+            if low and x not in keep:
+                sl = heapq.heappop(low)
+            elif high:
+                sl = heapq.heappop(high)
             else:
                 sl = next_slot
                 next_slot += 1
@@ -330,6 +455,8 @@ def schedule(P: Program, out: dict, G: int, copy_jac: bool, reverse: bool = Fals
     if nv > MAX_SLOTS:
         raise ValueError(f"program needs {nv} slots (max {MAX_SLOTS})")
     outputs = {"rhs": [resolve(P, r) for r in out["rhs"]]}
+    if jac:
+        outputs["jac"] = [resolve(P, x) for x in jac_roots]
     return Schedule(G, steps, slot, nv, outputs, None), args
 
 
@@ -383,9 +510,7 @@ def encode(P: Program, sch: Schedule, args, cidx: dict, sink: int, one: int, mze
                 x = riders[g]
                 op, a = P.nodes[x]
                 iop = INT_OP[op]
-                if op == "copy":  # E = -J
-                    ops = [c_true, operand(a[0], neg=True), c_true]
-                elif op == "and":
+                if op == "and":
                     ops = [operand(a[0]), operand(a[1]), c_false]
                 elif op == "or":
                     ops = [operand(a[0]), c_true, operand(a[1])]
@@ -404,16 +529,38 @@ def encode(P: Program, sch: Schedule, args, cidx: dict, sink: int, one: int, mze
     return words
 
 
-def generate(G: int, dag=None):
+# live-set limit of the list scheduler per G (chosen offline: the smallest slot
+# count among limits that do not add FP64 issue slots)
+SCHED_LIMIT = {8: 400, 16: 650, 32: None}
+# shared memory of one block (227 KiB) and the warps per block the slot arrays
+# allow, at most 16: at 16 lanes per cell (728 slots) 16 warps ran a 64^3 collapse
+# in 32.5 s on GB300, 17 warps in 34.3 s and 19 warps (register-limited) in 33.3 s
+SMEM_BLOCK = 232448
+MAX_WARPS = 16
+
+
+def warps_per_block(G: int, nv: int, nc: int) -> int:
+    """Warps of the cooperative advance's block: as many as the cells' slot
+    arrays and the constant table fit in one block's shared memory (one block
+    per SM), at most MAX_WARPS."""
+    ncpad = (nc + 1) & ~1
+    cells = (SMEM_BLOCK // 8 - ncpad) // nv
+    return max(1, min(MAX_WARPS, cells // (32 // G)))
+
+
+def generate(G: int, dag=None, limit="default"):
     """Programs jrhs and rhs for G lanes per cell: a dict with the encoded steps,
-    the output operands, the slot count and the constant table."""
+    the output operands, the slot count, the constant table and the warps per
+    block."""
     dag = dag or ir_io.load()
+    if limit == "default":
+        limit = SCHED_LIMIT.get(G)
     progs = {}
     consts = set()
     built = {}
     for kind in ("jrhs", "rhs"):
         P, out = build(dag, kind)
-        sch, args = schedule(P, out, G, copy_jac=(kind == "jrhs"))
+        sch, args = schedule(P, out, G, jac=(kind == "jrhs"), limit=limit)
         built[kind] = (P, out, sch, args)
         for x in range(len(P.nodes)):
             if P.nodes[x][0] == "const":
@@ -429,14 +576,18 @@ def generate(G: int, dag=None):
     for kind, (P, out, sch, args) in built.items():
         words = encode(P, sch, args, cidx, sink, one, mzero)
 
-        def outop(r):
+        def outop(r, negate=False):
             b, neg, ab = r
+            if negate:
+                neg = not neg
             v = (cidx[P.nodes[b][1][0]] | OPF_CONST) if P.nodes[b][0] == "const" else sch.slot[b]
             return v | (OPF_NEG if neg else 0) | (OPF_ABS if ab else 0)
 
         progs[kind] = {"words": words, "rhs_out": [outop(r) for r in sch.outputs["rhs"]],
                        "nsteps": len(sch.steps), "stats": stats(sch)}
-    return {"G": G, "nv": nv, "consts": ctab, "progs": progs}
+        if "jac" in sch.outputs:  # E = -J, entry r * 15 + c
+            progs[kind]["jac_out"] = [outop(r, negate=True) for r in sch.outputs["jac"]]
+    return {"G": G, "nv": nv, "consts": ctab, "progs": progs, "warps": warps_per_block(G, nv, len(ctab))}
 
 
 def stats(sch: Schedule) -> dict:
@@ -458,6 +609,7 @@ def emit_header(G: int, gen: dict, digest: str) -> str:
         f"constexpr int kG = {G};",
         f"constexpr int kNV = {gen['nv']};",
         f"constexpr int kNC = {len(gen['consts'])};",
+        f"constexpr int kWarps = {gen['warps']};  // warps per block: the slot arrays that fit in shared memory",
     ]
     for kind, pr in gen["progs"].items():
         st = pr["stats"]
@@ -477,6 +629,12 @@ def emit_header(G: int, gen: dict, digest: str) -> str:
         lines.append("};")
         lines.append(f"static __device__ const uint16_t k{K}Out[15] = {{" +
                      ", ".join(str(v) for v in pr["rhs_out"]) + "};")
+        if "jac_out" in pr:
+            lines.append(f"static __device__ const uint16_t k{K}Jac[225] = {{")
+            jo = pr["jac_out"]
+            for i in range(0, 225, 15):
+                lines.append("    " + ", ".join(str(v) for v in jo[i:i + 15]) + ",")
+            lines.append("};")
     lines.append(f"}} }}  // namespace wr::coop{G}")
     return "\n".join(lines) + "\n"
 
