@@ -678,7 +678,8 @@ def profile_policy(args):
     build.build_all()
     cells = wr.make_grid(args.grid)
     policy = wr.POLICY_GRIDWIDE_CTA32 if args.profile_policy == "cta32" else wr.POLICY_GRIDWIDE_INDEPENDENT
-    with wr.Context(len(cells)) as ctx:
+    math_mode = wr.MATH_CUDA if args.math == "cuda" else wr.MATH_PORTABLE
+    with wr.Context(len(cells), 0, math_mode) as ctx:
         ctx.set_policy(policy)
         ctx.upload(cells)
         rc, _ = ctx.run(True)
@@ -694,6 +695,8 @@ def profile_steps(args):
     cells = wr.make_grid(args.grid)
     math_mode = wr.MATH_CUDA if args.math == "cuda" else wr.MATH_PORTABLE
     with wr.Context(len(cells), 0, math_mode) as ctx:
+        if args.variant is not None:
+            ctx.set_variant(args.variant)
         ctx.upload(cells)
         grid_time, done = 0.0, 0
         for step in range(args.profile_steps):
@@ -734,6 +737,8 @@ def main():
     ap.add_argument("--batch-tune-steps", type=int, default=3)
     ap.add_argument("--profile-policy", choices=("independent", "cta32"), default=None,
                     help="profiling driver: one full collapse with this policy through wr_run, print nothing, exit")
+    ap.add_argument("--variant", type=int, default=None,
+                    help="advance launch shape of --profile-steps (wr_set_advance_variant; default: the library's)")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiling driver: run this many outer steps host-stepped, print nothing, exit")
     args = ap.parse_args()
