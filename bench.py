@@ -565,6 +565,8 @@ def run_gb300(args, rank, ws, local, tdist):
     forms = {}
 
     def budget_ok(name, est_s):
+        if args.forms is not None and name not in args.forms.split(","):
+            return False
         left = args.budget_s - (time.perf_counter() - t_start)
         if est_s > left:
             forms[name] = {"skipped": f"wall-clock budget: needs ~{est_s:.0f} s, {left:.0f} s left of --budget-s"}
@@ -726,6 +728,9 @@ def main():
     ap.add_argument("--forms-batch-scale", type=float, default=0.5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the forms after the timed region")
+    ap.add_argument("--forms", default=None,
+                    help="comma-separated forms to run after the timed region (default: all that fit --budget-s): "
+                         "reference_cuda_kernel, portable_math, cta32_policy, differentiation, batching, precision")
     ap.add_argument("--probe-fp64", action="store_true",
                     help="print this GPU's FP64 issue interval per warp count and the FMA peak, exit")
     ap.add_argument("--diff", action="store_true",

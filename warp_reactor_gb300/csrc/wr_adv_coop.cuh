@@ -16,21 +16,24 @@ namespace cp = WR_CAT(coop, WR_COOP_G);
 
 struct Tab {
     static constexpr int kNV = cp::kNV;
-    static constexpr int kNC = cp::kNC;
-    static constexpr int kNCPad = (cp::kNC + 1) & ~1;
+    static constexpr int kNR = cp::kNR;
     static constexpr int kJSteps = cp::kJRHSSteps;
     static constexpr int kRSteps = cp::kRHSSteps;
     static __device__ __forceinline__ const ulonglong2* jprog() { return cp::kJRHSProg; }
+    static __device__ __forceinline__ const uint64_t* jlit() { return cp::kJRHSLit; }
     static __device__ __forceinline__ const ulonglong2* rprog() { return cp::kRHSProg; }
+    static __device__ __forceinline__ const uint64_t* rlit() { return cp::kRHSLit; }
     static __device__ __forceinline__ const uint16_t* jout() { return cp::kJRHSOut; }
     static __device__ __forceinline__ const uint16_t* jac() { return cp::kJRHSJac; }
     static __device__ __forceinline__ const uint16_t* rout() { return cp::kRHSOut; }
-    static __device__ __forceinline__ const uint64_t* cst() { return cp::kConst; }
+    static __device__ __forceinline__ const uint64_t* vconst() { return cp::kVConst; }
 };
+static_assert(Tab::kJSteps % 4 == 0 && Tab::kRSteps % 4 == 0, "programs are padded to groups of four steps");
+static_assert(coop::kRes + Tab::kNR <= Tab::kNV, "reserved constants lie inside the slot array");
 
 constexpr int kG = WR_COOP_G;
 constexpr int kW = cp::kWarps;
-constexpr size_t kSmem = (static_cast<size_t>(Tab::kNCPad) + static_cast<size_t>(kW) * (32 / kG) * Tab::kNV) * 8;
+constexpr size_t kSmem = static_cast<size_t>(kW) * (32 / kG) * Tab::kNV * 8;
 static_assert(kSmem <= 232448, "cooperative advance: shared memory of one block exceeds 227 KiB");
 }  // namespace
 
@@ -53,7 +56,7 @@ cudaError_t WR_CAT(launch_advance_coop, WR_COOP_G)(int math_cuda, int blocks, cu
 
 namespace {
 constexpr int kDiagWarps = 4;
-constexpr size_t kDiagNetSmem = (static_cast<size_t>(Tab::kNCPad) + kDiagWarps * (32 / kG) * Tab::kNV) * 8;
+constexpr size_t kDiagNetSmem = static_cast<size_t>(kDiagWarps) * (32 / kG) * Tab::kNV * 8;
 constexpr size_t kDiagLuSmem = static_cast<size_t>(kDiagWarps) * (32 / kG) * NEQ * NEQ * 8;
 }  // namespace
 

@@ -50,9 +50,17 @@ constexpr int kQBurnOK = -4;   // burned successfully: k_commit commits it
 namespace coop {
 
 enum { C_NONE = 0, C_FMA = 1, C_EXP = 2, C_LOG = 3, C_SQRT = 4, C_DIV = 5 };
-enum { I_SEL = 0, I_LE = 1, I_LT = 2 };
+enum { I_SEL = 0, I_LE = 1, I_LT = 2, I_SGN = 3 };
+// flags in the low three bits of the 16-bit byte-offset fields of a step
+enum : uint32_t {
+    FL_NEG = 1u, FL_ABS = 2u, FL_SWAP = 4u,  // X, Y: argument modifiers; Y: divide V[Y] ^ L by V[X]
+    FL_INT = 1u, FL_SPECIAL = 2u,            // Z: integer nodes / comparisons or sign ops in the step
+    FL_SABS = 4u                             // integer destination of I_SGN: clear the sign (else flip)
+};
 constexpr int kE = 0;        // iteration matrix slots [0, 225)
 constexpr int kY = 225;      // program inputs y[0..14]
+constexpr int kRes = 240;    // reserved constants [240, 240 + Tab::kNR)
+constexpr uint32_t kOff = 0xfff8u;
 constexpr uint64_t kSign = 0x8000000000000000ULL;
 constexpr uint64_t kAbs = 0x7fffffffffffffffULL;
 constexpr uint64_t kInfBits = 0x7ff0000000000000ULL;
@@ -60,10 +68,10 @@ constexpr uint64_t kInfBits = 0x7ff0000000000000ULL;
 __device__ __forceinline__ double dbl(uint64_t u) { return __longlong_as_double(static_cast<long long>(u)); }
 __device__ __forceinline__ uint64_t bits(double d) { return static_cast<uint64_t>(__double_as_longlong(d)); }
 
-// operand: slot (12 bits) | constant table (bit 12) | negate (bit 13) | abs (bit 14)
-__device__ __forceinline__ uint64_t fetch(const uint64_t* V, const uint64_t* C, uint32_t op) {
-    const uint64_t* base = (op & 0x1000u) ? C : V;
-    uint64_t v = base[op & 0xfffu];
+// output operand (the RHS and Jacobian tables): slot (12 bits) | negate (bit 13) |
+// abs (bit 14); constants sit in reserved slots
+__device__ __forceinline__ uint64_t fetch(const uint64_t* V, uint32_t op) {
+    uint64_t v = V[op & 0xfffu];
     v = (op & 0x4000u) ? (v & kAbs) : v;
     v = (op & 0x2000u) ? (v ^ kSign) : v;
     return v;
@@ -82,16 +90,10 @@ __device__ __forceinline__ void sts64(uint32_t addr, uint64_t v) {
 __device__ __forceinline__ void group_sync(unsigned gmask) {
     asm volatile("bar.warp.sync %0;" ::"r"(gmask) : "memory");
 }
-// operand fetch on shared-window addresses: the slot's byte offset in the cell's
-// slot array or the constant table, then the sign modifiers on the high word
-// (abs clears bit 63, negate flips it)
-__device__ __forceinline__ uint64_t fetch_s(uint32_t vb, uint32_t cb, uint32_t op) {
-    const uint32_t addr = ((op & 0x1000u) ? cb : vb) + ((op & 0xfffu) << 3);
-    const uint64_t v = lds64(addr);
-    const uint32_t lo = static_cast<uint32_t>(v);
-    uint32_t hi = static_cast<uint32_t>(v >> 32);
-    hi = (hi & ~((op << 17) & 0x80000000u)) ^ ((op << 18) & 0x80000000u);
-    return (static_cast<uint64_t>(hi) << 32) | lo;
+// sign modifiers of an exp/log/sqrt/div argument (abs, then negate)
+__device__ __forceinline__ uint64_t modify(uint64_t v, uint32_t fl) {
+    v = (fl & FL_ABS) ? (v & kAbs) : v;
+    return (fl & FL_NEG) ? (v ^ kSign) : v;
 }
 
 // IEEE a <= b and a < b on bit patterns: false when either is NaN, -0 == +0
@@ -121,86 +123,97 @@ struct StepMath {
     static __device__ __noinline__ double sqrt(double x) { return M::sqrt(x); }
 };
 
+// One step of one lane.  e.x: main word X | Y | Z | D (16-bit byte offsets into
+// the cell's slot array at shared address vb, flags in their low three bits);
+// e.y: integer word A | B | C | D2; lit: the lane's literal, XOR-ed into V[Y].
+// An FMA step's operand offsets carry no flags (the generator guarantees it), so
+// they are added to vb as they are.
 template <class M>
-__device__ __forceinline__ void exec_step(const ulonglong2 e, uint32_t vb, uint32_t cb) {
-    const uint64_t mw = e.x;
-    const uint32_t lo = static_cast<uint32_t>(mw), hi = static_cast<uint32_t>(mw >> 32);
-    const uint32_t cls = (hi >> 28) & 7u;
+__device__ __forceinline__ void exec_step(const ulonglong2 e, const uint64_t lit, uint32_t vb) {
+    const uint32_t w0 = static_cast<uint32_t>(e.x), w1 = static_cast<uint32_t>(e.x >> 32);
+    const uint32_t cls = (w1 >> 16) & 7u;
+    const uint32_t dst = vb + ((w1 >> 16) & kOff);
     if (cls == C_FMA) {
-        const double a = dbl(fetch_s(vb, cb, lo & 0x7fffu));
-        const double b = dbl(fetch_s(vb, cb, lo >> 16));
-        const double c = dbl(fetch_s(vb, cb, hi & 0xffffu));
-        sts64(vb + (((hi >> 16) & 0xfffu) << 3), bits(__fma_rn(a, b, c)));
+        const double a = dbl(lds64(vb + (w0 & 0xffffu)));
+        const double b = dbl(lds64(vb + (w0 >> 16)) ^ lit);
+        const double c = dbl(lds64(vb + (w1 & kOff)));
+        sts64(dst, bits(__fma_rn(a, b, c)));
     } else if (cls != C_NONE) {
-        const double a = dbl(fetch_s(vb, cb, lo & 0x7fffu));
+        const uint32_t yf = w0 >> 16;
+        const uint64_t y = modify(lds64(vb + (yf & kOff)) ^ lit, yf);
         double r;
         if (cls == C_DIV) {
-            r = ddiv(a, dbl(fetch_s(vb, cb, lo >> 16)));
+            const uint64_t x = modify(lds64(vb + (w0 & kOff)), w0);
+            const bool sw = (yf & FL_SWAP) != 0;
+            r = ddiv(dbl(sw ? y : x), dbl(sw ? x : y));
         } else if (cls == C_EXP) {
-            r = StepMath<M>::exp(a);
+            r = StepMath<M>::exp(dbl(y));
         } else if (cls == C_LOG) {
-            r = StepMath<M>::log(a);
+            r = StepMath<M>::log(dbl(y));
         } else {
-            r = StepMath<M>::sqrt(a);
+            r = StepMath<M>::sqrt(dbl(y));
         }
-        sts64(vb + (((hi >> 16) & 0xfffu) << 3), bits(r));
+        sts64(dst, bits(r));
     }
-    if (hi >> 31) {
-        const uint32_t ilo = static_cast<uint32_t>(e.y), ihi = static_cast<uint32_t>(e.y >> 32);
-        const uint64_t A = fetch_s(vb, cb, ilo & 0xffffu);
-        const uint64_t B = fetch_s(vb, cb, ilo >> 16);
-        const uint64_t Cc = fetch_s(vb, cb, ihi & 0xffffu);
-        uint64_t r = A != 0 ? B : Cc;
-        if (lo & 0x8000u) {  // the step carries comparisons (uniform over the warp)
-            const uint32_t iop = ihi >> 28;
+    if (w1 & FL_INT) {  // the step carries integer nodes (uniform over the warp)
+        const uint32_t i0 = static_cast<uint32_t>(e.y), i1 = static_cast<uint32_t>(e.y >> 32);
+        const uint64_t A = lds64(vb + (i0 & 0xffffu));
+        const uint64_t B = lds64(vb + (i0 >> 16));
+        const uint64_t C = lds64(vb + (i1 & 0xffffu));
+        uint64_t r = A != 0 ? B : C;
+        if (w1 & FL_SPECIAL) {  // comparisons or sign operations (uniform over the warp)
+            const uint32_t iop = (i1 >> 16) & 3u;
             r = iop == I_LE ? ble(A, B) : r;
             r = iop == I_LT ? blt(A, B) : r;
+            r = iop == I_SGN ? (((i1 >> 16) & FL_SABS) ? (A & kAbs) : (A ^ kSign)) : r;
         }
-        sts64(vb + (((ihi >> 16) & 0xfffu) << 3), r);
+        sts64(vb + ((i1 >> 16) & kOff), r);
     }
 }
 
-// One generated program on the group's cell: steps of (main word, integer word)
-// per lane; the group synchronises after every step.  One out-of-line copy serves
-// every call site (the instruction cache holds one loop), unrolled by four with the
-// next four steps' table entries loaded while the current four execute: the tables
-// (~100-200 KB per G) live mostly in L2, since shared memory takes most of L1.
+// One generated program on the group's cell: the steps' words per lane; the group
+// synchronises after every step.  One out-of-line copy serves every call site (the
+// instruction cache holds one loop).  The step count is a multiple of four and the
+// tables carry four idle steps more, so the loop runs four steps per iteration and
+// loads each step's words four steps before it executes them (the tables, ~100-200
+// KB per G, live mostly in L2: shared memory takes most of L1).
 template <class M, int G>
-__device__ __noinline__ void run_prog(const ulonglong2* __restrict__ prog, int nsteps, int gl, uint64_t* V,
-                                      const uint64_t* C, unsigned gmask) {
+__device__ __noinline__ void run_prog(const ulonglong2* __restrict__ prog, const uint64_t* __restrict__ lits,
+                                      int nsteps, int gl, uint64_t* V, unsigned gmask) {
     const uint32_t vb = static_cast<uint32_t>(__cvta_generic_to_shared(V));
-    const uint32_t cb = static_cast<uint32_t>(__cvta_generic_to_shared(C));
     const ulonglong2* p = prog + gl;
-    const ulonglong2 zero = make_ulonglong2(0, 0);
-    ulonglong2 e0 = nsteps > 0 ? __ldg(p) : zero;
-    ulonglong2 e1 = nsteps > 1 ? __ldg(p + G) : zero;
-    ulonglong2 e2 = nsteps > 2 ? __ldg(p + 2 * G) : zero;
-    ulonglong2 e3 = nsteps > 3 ? __ldg(p + 3 * G) : zero;
+    const uint64_t* q = lits + gl;
+    ulonglong2 e0 = __ldg(p), e1 = __ldg(p + G), e2 = __ldg(p + 2 * G), e3 = __ldg(p + 3 * G);
+    uint64_t l0 = __ldg(q), l1 = __ldg(q + G), l2 = __ldg(q + 2 * G), l3 = __ldg(q + 3 * G);
 #pragma unroll 1
     for (int s = 0; s < nsteps; s += 4) {
-        const ulonglong2 n0 = s + 4 < nsteps ? __ldg(p + (s + 4) * G) : zero;
-        const ulonglong2 n1 = s + 5 < nsteps ? __ldg(p + (s + 5) * G) : zero;
-        const ulonglong2 n2 = s + 6 < nsteps ? __ldg(p + (s + 6) * G) : zero;
-        const ulonglong2 n3 = s + 7 < nsteps ? __ldg(p + (s + 7) * G) : zero;
-        exec_step<M>(e0, vb, cb);
+        p += 4 * G;
+        q += 4 * G;
+        exec_step<M>(e0, l0, vb);
+        e0 = __ldg(p);
+        l0 = __ldg(q);
         group_sync(gmask);
-        if (s + 1 < nsteps) {
-            exec_step<M>(e1, vb, cb);
-            group_sync(gmask);
-        }
-        if (s + 2 < nsteps) {
-            exec_step<M>(e2, vb, cb);
-            group_sync(gmask);
-        }
-        if (s + 3 < nsteps) {
-            exec_step<M>(e3, vb, cb);
-            group_sync(gmask);
-        }
-        e0 = n0;
-        e1 = n1;
-        e2 = n2;
-        e3 = n3;
+        exec_step<M>(e1, l1, vb);
+        e1 = __ldg(p + G);
+        l1 = __ldg(q + G);
+        group_sync(gmask);
+        exec_step<M>(e2, l2, vb);
+        e2 = __ldg(p + 2 * G);
+        l2 = __ldg(q + 2 * G);
+        group_sync(gmask);
+        exec_step<M>(e3, l3, vb);
+        e3 = __ldg(p + 3 * G);
+        l3 = __ldg(q + 3 * G);
+        group_sync(gmask);
     }
+}
+
+// the reserved constants of the programs into the group's slot array (once per
+// launch: no program writes them)
+template <int G, class Tab>
+__device__ __forceinline__ void init_reserved(uint64_t* V, int gl, unsigned gmask) {
+    for (int i = gl; i < Tab::kNR; i += G) V[kRes + i] = Tab::vconst()[i];
+    __syncwarp(gmask);
 }
 
 // lu_decomposition<15> (reproducer.cpp:96-151) by the G lanes of a group on the
@@ -335,31 +348,30 @@ __device__ __forceinline__ void store_inputs(uint64_t* V, const double (&v)[K], 
 }
 
 template <int G, int K>
-__device__ __forceinline__ void load_outputs(const uint64_t* V, const uint64_t* C, const uint16_t* out, double (&v)[K],
-                                             int gl) {
+__device__ __forceinline__ void load_outputs(const uint64_t* V, const uint16_t* out, double (&v)[K], int gl) {
 #pragma unroll
     for (int t = 0; t < K; ++t) {
         const int c = gl + t * G;
-        v[t] = c < NEQ ? dbl(fetch(V, C, out[c])) : 0.0;
+        v[t] = c < NEQ ? dbl(fetch(V, out[c])) : 0.0;
     }
 }
 
 // E = -J into the matrix slots after the Jacobian program.  The program uses the
 // matrix slots as scratch and keeps its results (the Jacobian entries and the
 // RHS) above them; the generated table names, per matrix entry r * 15 + c, the
-// slot or constant that holds J(r, c) with the negation as an operand modifier.
+// slot (a reserved one for a constant entry) that holds J(r, c) with the negation
+// as an operand modifier.
 template <int G>
-__device__ __forceinline__ void gather_matrix(uint64_t* V, const uint64_t* C, const uint16_t* jac, int gl,
-                                              unsigned gmask) {
+__device__ __forceinline__ void gather_matrix(uint64_t* V, const uint16_t* jac, int gl, unsigned gmask) {
 #pragma unroll 1
-    for (int i = gl; i < NEQ * NEQ; i += G) V[kE + i] = fetch(V, C, jac[i]);
+    for (int i = gl; i < NEQ * NEQ; i += G) V[kE + i] = fetch(V, jac[i]);
     __syncwarp(gmask);
 }
 
 // Generated tables of one G, supplied by the translation unit that includes the
 // generated header (one unit per G keeps the large initialisers apart).
-//   Tab::kNV, Tab::kNC, Tab::kJSteps, Tab::kRSteps and device accessors
-//   jprog(), rprog(), jout(), jac(), rout(), cst().
+//   Tab::kNV, Tab::kNR, Tab::kJSteps, Tab::kRSteps and device accessors
+//   jprog(), jlit(), rprog(), rlit(), jout(), jac(), rout(), vconst().
 
 }  // namespace coop
 
@@ -371,16 +383,14 @@ __global__ void __launch_bounds__(W * 32, 1) k_advance_coop(DevState s, StepCtl*
     constexpr int K = (NEQ + G - 1) / G;
     constexpr int SLOTS = 32 / G;
     extern __shared__ uint64_t sm[];
-    uint64_t* C = sm;
-    for (int i = threadIdx.x; i < Tab::kNC; i += W * 32) C[i] = Tab::cst()[i];
-    __syncthreads();
     if (ctl->all_stop) return;
     const int lane = threadIdx.x & 31;
     const int slot = lane / G;
     const int gl = lane % G;
     const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (slot * G));
-    uint64_t* V = sm + Tab::kNCPad + static_cast<size_t>((threadIdx.x >> 5) * SLOTS + slot) * Tab::kNV;
+    uint64_t* V = sm + static_cast<size_t>((threadIdx.x >> 5) * SLOTS + slot) * Tab::kNV;
     double* E = reinterpret_cast<double*>(V + kE);
+    init_reserved<G, Tab>(V, gl, gmask);
     const int n = s.n;
     const unsigned int queued = ctl->queued;
 
@@ -474,9 +484,9 @@ __global__ void __launch_bounds__(W * 32, 1) k_advance_coop(DevState s, StepCtl*
         // ---- one ROS2S attempt, reproducer.cpp:7259-7345
         store_inputs<G, K>(V, y, gl);
         __syncwarp(gmask);
-        run_prog<M, G>(Tab::jprog(), Tab::kJSteps, gl, V, C, gmask);
-        load_outputs<G, K>(V, C, Tab::jout(), f0, gl);
-        gather_matrix<G>(V, C, Tab::jac(), gl, gmask);
+        run_prog<M, G>(Tab::jprog(), Tab::jlit(), Tab::kJSteps, gl, V, gmask);
+        load_outputs<G, K>(V, Tab::jout(), f0, gl);
+        gather_matrix<G>(V, Tab::jac(), gl, gmask);
         if (L.fresh) L.n_jac += 1;
         L.fresh = false;
         const double h = L.h;
@@ -526,9 +536,9 @@ __global__ void __launch_bounds__(W * 32, 1) k_advance_coop(DevState s, StepCtl*
             }
             store_inputs<G, K>(V, yn, gl);
             __syncwarp(gmask);
-            run_prog<M, G>(Tab::rprog(), Tab::kRSteps, gl, V, C, gmask);
+            run_prog<M, G>(Tab::rprog(), Tab::rlit(), Tab::kRSteps, gl, V, gmask);
             double dy[K];
-            load_outputs<G, K>(V, C, Tab::rout(), dy, gl);
+            load_outputs<G, K>(V, Tab::rout(), dy, gl);
 #pragma unroll
             for (int t = 0; t < K; ++t) w[t] += dy[t];
             solve_coop<G, K>(E, ip, w, gl, gmask);
@@ -546,9 +556,9 @@ __global__ void __launch_bounds__(W * 32, 1) k_advance_coop(DevState s, StepCtl*
             __syncwarp(gmask);  // every lane has read the stage-2 outputs
             store_inputs<G, K>(V, yn, gl);
             __syncwarp(gmask);
-            run_prog<M, G>(Tab::rprog(), Tab::kRSteps, gl, V, C, gmask);
+            run_prog<M, G>(Tab::rprog(), Tab::rlit(), Tab::kRSteps, gl, V, gmask);
             double dy[K];
-            load_outputs<G, K>(V, C, Tab::rout(), dy, gl);
+            load_outputs<G, K>(V, Tab::rout(), dy, gl);
 #pragma unroll
             for (int t = 0; t < K; ++t) w[t] += dy[t];
             solve_coop<G, K>(E, ip, w, gl, gmask);
@@ -631,16 +641,14 @@ __global__ void k_diag_coop_network(int n, const double* __restrict__ y, double*
     constexpr int K = (NEQ + G - 1) / G;
     constexpr int SLOTS = 32 / G;
     extern __shared__ uint64_t sm[];
-    uint64_t* C = sm;
-    for (int i = threadIdx.x; i < Tab::kNC; i += blockDim.x) C[i] = Tab::cst()[i];
-    __syncthreads();
     const int lane = threadIdx.x & 31, slot = lane / G, gl = lane % G;
     const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (slot * G));
     const int warp = threadIdx.x >> 5;
     const int cell = (blockIdx.x * (blockDim.x >> 5) + warp) * SLOTS + slot;
     if (cell >= n) return;
-    uint64_t* V = sm + Tab::kNCPad + static_cast<size_t>(warp * SLOTS + slot) * Tab::kNV;
+    uint64_t* V = sm + static_cast<size_t>(warp * SLOTS + slot) * Tab::kNV;
     const double* E = reinterpret_cast<const double*>(V + kE);
+    init_reserved<G, Tab>(V, gl, gmask);
     double yy[K], out[K];
 #pragma unroll
     for (int t = 0; t < K; ++t) {
@@ -649,9 +657,9 @@ __global__ void k_diag_coop_network(int n, const double* __restrict__ y, double*
     }
     store_inputs<G, K>(V, yy, gl);
     __syncwarp(gmask);
-    run_prog<M, G>(Tab::jprog(), Tab::kJSteps, gl, V, C, gmask);
-    load_outputs<G, K>(V, C, Tab::jout(), out, gl);
-    gather_matrix<G>(V, C, Tab::jac(), gl, gmask);
+    run_prog<M, G>(Tab::jprog(), Tab::jlit(), Tab::kJSteps, gl, V, gmask);
+    load_outputs<G, K>(V, Tab::jout(), out, gl);
+    gather_matrix<G>(V, Tab::jac(), gl, gmask);
     for (int i = gl; i < NEQ * NEQ; i += G) J[static_cast<size_t>(cell) * NEQ * NEQ + i] = -E[i];
 #pragma unroll
     for (int t = 0; t < K; ++t) {
@@ -661,8 +669,8 @@ __global__ void k_diag_coop_network(int n, const double* __restrict__ y, double*
     __syncwarp(gmask);
     store_inputs<G, K>(V, yy, gl);
     __syncwarp(gmask);
-    run_prog<M, G>(Tab::rprog(), Tab::kRSteps, gl, V, C, gmask);
-    load_outputs<G, K>(V, C, Tab::rout(), out, gl);
+    run_prog<M, G>(Tab::rprog(), Tab::rlit(), Tab::kRSteps, gl, V, gmask);
+    load_outputs<G, K>(V, Tab::rout(), out, gl);
 #pragma unroll
     for (int t = 0; t < K; ++t) {
         const int c = gl + t * G;

@@ -4,35 +4,52 @@ The cooperative kernel evaluates one cell's network with ``G`` lanes (``G`` = 8,
 16 or 32 lanes per cell, ``32/G`` cells per warp).  The values of the evaluation
 live in the cell's shared-memory slot array ``V``; the work is a *program*: a
 sequence of steps, each executed by every lane of the warp, in which lane ``g``
-computes one node of the DAG from operands gathered out of ``V`` (or the block's
-constant table) and stores it back into ``V``.  Between steps the warp
+computes one node of the DAG from operands gathered out of ``V`` and stores it
+back into ``V``.  Between steps the warp
 synchronises, so a step may use any value produced by an earlier step.
 
-Step format (per lane, two 64-bit words):
+Step format (per lane, three 64-bit words; every address is the byte offset of a
+slot in the cell's own slot array, so the device adds it to one base):
 
-* main word: class (3 bits: none, fma, exp, log, sqrt, div), "has integer part"
-  (1 bit), destination slot (12 bits) and three operands (16 bits each; bit 15 of
-  the first says "the integer part holds comparisons");
-* integer word: op (select, le, lt), destination and three operands.  Every
-  step may carry up to ``G`` integer nodes beside its main node, so comparisons,
-  selects and boolean logic ride along with the floating-point work instead of
-  taking steps of their own.  Boolean logic and copies are selects A ? B : C with
-  the boolean constants as operands: a and b = a ? b : 0, a or b = a ? 1 : b,
-  not a = a ? 0 : 1, copy x = 1 ? x : 1.
+* main word: four 16-bit fields X | Y | Z | D.  An FMA step computes
+  ``V[D] = fma(V[X], V[Y] ^ L, V[Z])``; exp, log and sqrt take ``V[Y] ^ L`` and
+  division ``V[X] / (V[Y] ^ L)`` (operands swapped by a flag).  The low three bits
+  of a field are free (slots are 8 bytes) and hold flags: the step's class in D,
+  "the step has integer nodes" and "they include comparisons or sign operations"
+  in Z (both uniform over the step), and the sign modifiers of exp/log/sqrt/div
+  arguments in X and Y;
+* integer word: four 16-bit fields A | B | C | D2, one integer node
+  ``V[D2] = A != 0 ? B : C`` (or a comparison A <= B, A < B, or a sign operation
+  on A; the op in the low bits of D2).  Every step may carry up to ``G`` integer
+  nodes beside its main node, so comparisons, selects and boolean logic ride
+  along with the floating-point work instead of taking steps of their own.
+  Boolean logic and copies are selects over the boolean constants:
+  a and b = a ? b : 0, a or b = a ? 1 : b, not a = a ? 0 : 1;
+* literal word L: the lane's constant operand, XOR-ed into ``V[Y]`` (``Y`` then
+  names a slot holding +0.0, so the operand is the constant); 0 otherwise.
 
-Operand: slot index (12 bits), "constant table" flag, negate flag and absolute
-value flag.  ``neg`` and ``abs`` nodes of the DAG are therefore never computed:
-they become operand modifiers (a sign-bit operation on the integer pipe, exact).
+Constants therefore never need a table of their own: a network coefficient is the
+literal of the lane that uses it, and the few constants that integer nodes and the
+outputs read (booleans, the neutral operands 1, -1 and -0, comparison limits) sit
+in reserved slots of every cell's array, written once per launch.
 
-Arithmetic: every ``add``, ``sub`` and ``mul`` is one fused multiply-add with an
-exact neutral operand, so one FP64 instruction class serves all three and lanes of
-a step may mix them.  Each is the same correctly rounded binary64 result as the
-separate operation:
+Operand modifiers: ``neg`` and ``abs`` nodes of the DAG are never computed.  On an
+exp/log/sqrt/div argument they are flags; an FMA or integer node that reads a
+negated or absolute value reads it from an integer sign node (``sneg``/``sabs``,
+a sign-bit operation, exact) that the generator inserts; on a constant they are
+folded into the constant.
+
+Arithmetic: every ``add``, ``sub`` and ``mul`` is one fused multiply-add with
+exact neutral operands, so one FP64 instruction class serves all three and lanes
+of a step may mix them.  Each is the same correctly rounded binary64 result as
+the separate operation:
 
 * ``a * b  == fma(a, b, -0.0)`` (adding -0 never changes a product, and keeps the
-  sign of a zero product);
-* ``a + b  == fma(a, 1.0, b)`` (a * 1 is exact, then one rounding of the sum);
-* ``a - b  == fma(a, 1.0, -b)`` (IEEE defines a - b as a + (-b)).
+  sign of a zero product); ``a * K == fma(a, K, -0.0)``;
+* ``a + b  == fma(a, 1.0, b)``, ``a + K == fma(1.0, K, a)`` (the product is
+  exact, then one rounding of the sum; IEEE addition commutes);
+* ``a - b  == fma(b, -1.0, a)`` (IEEE defines a - b as a + (-b), and b * -1 is
+  exactly -b), ``a - K == fma(1.0, -K, a)``, ``K - b == fma(b, -1.0, K)``.
 
 Comparisons are done on the bit patterns (exact IEEE ordering: NaN unordered,
 -0 == +0), booleans are stored as the integers 0/1, selects copy bit patterns.
@@ -49,7 +66,8 @@ Two programs are generated per ``G``:
 * ``rhs``: the same prologue and the RHS only.
 
 Slot map of a cell: ``[0, 225)`` the iteration matrix, ``[225, 240)`` the
-inputs, then scratch; the last slot is a write sink for idle lanes.  The Jacobian
+inputs, ``[240, 240 + R)`` the reserved constants, then scratch; the last slot is
+a write sink for idle lanes.  The Jacobian
 program runs before the matrix is formed, so it uses the matrix slots as scratch
 too and keeps its results above them; the RHS program runs while the matrix holds
 the LU factors and never writes it.  Slots are allocated by a linear scan over
@@ -73,14 +91,16 @@ from . import ir_io
 
 # main classes
 C_NONE, C_FMA, C_EXP, C_LOG, C_SQRT, C_DIV = 0, 1, 2, 3, 4, 5
-# integer ops
 # integer ops: every copy / and / or / not / select is one select A ? B : C (with
-# boolean constants 0 and 1 as operands), comparisons are the other two
-I_SEL, I_LE, I_LT = 0, 1, 2
+# the boolean constants 0 and 1 as operands); comparisons A <= B, A < B; a sign
+# operation on A (flip the sign bit, or clear it)
+I_SEL, I_LE, I_LT, I_SGN = 0, 1, 2, 3
 
+FMA_OPS = ("add", "sub", "mul")
 MAIN_CLASS = {"add": C_FMA, "sub": C_FMA, "mul": C_FMA, "exp": C_EXP, "cexp": C_EXP, "log": C_LOG,
               "clog": C_LOG, "sqrt": C_SQRT, "csqrt": C_SQRT, "div": C_DIV}
-INT_OP = {"le": I_LE, "lt": I_LT, "and": I_SEL, "or": I_SEL, "not": I_SEL, "sel": I_SEL}
+INT_OP = {"le": I_LE, "lt": I_LT, "and": I_SEL, "or": I_SEL, "not": I_SEL, "sel": I_SEL, "sneg": I_SGN,
+          "sabs": I_SGN}
 # FP64 issue slots of one step of each class (measured call throughput of CUDA's
 # exp/log/sqrt on GB300; division runs on the integer pipe)
 STEP_COST = {C_FMA: 1.0, C_EXP: 19.0, C_LOG: 29.0, C_SQRT: 9.0, C_DIV: 0.5}
@@ -89,14 +109,22 @@ LATENCY = {C_FMA: 1.0, C_EXP: 3.0, C_LOG: 3.0, C_SQRT: 2.0, C_DIV: 2.0, "int": 1
 
 E_SLOTS = 225
 Y_BASE = 225
+RES_BASE = 240
 SLOT_BITS = 12
 MAX_SLOTS = 1 << SLOT_BITS
-OPF_CONST = 1 << 12
+# output operands (the RHS and Jacobian tables): slot | negate | absolute value
 OPF_NEG = 1 << 13
 OPF_ABS = 1 << 14
-# bit 15 of the main word (unused by its first operand): the step's integer part
-# holds comparisons, so only such steps run the comparison code
-OPF_STEP_CMP = 1 << 15
+# flags in the low bits of the 16-bit address fields (slots are 8 bytes)
+FL_NEG, FL_ABS, FL_SWAP = 1, 2, 4        # X, Y: argument modifiers; Y: divide V[Y] ^ L by V[X]
+FL_INT, FL_SPECIAL = 1, 2                # Z: the step has integer nodes / comparisons or sign ops
+FL_SABS = 4                              # D2 of I_SGN: clear the sign bit (else flip it)
+# steps are executed in groups of four, and the tables carry four idle steps more
+# so that the device may load four steps ahead without a bound check
+STEP_ALIGN = 4
+PREFETCH_PAD = 4
+SIGN = 1 << 63
+ABS = SIGN - 1
 
 FLOOR = 1.0e-100  # reproducer.cpp:231
 # species masses, reproducer.cpp:233-248 (the literals of wr_physics.cuh)
@@ -274,6 +302,73 @@ def resolve(P: Program, x: int):
     return x, neg, ab
 
 
+def lower(P: Program) -> None:
+    """Take operand modifiers off the operands of FMA and integer nodes, whose step
+    format reads plain slots: a negated or absolute operand becomes an integer
+    sign node (``sabs`` then ``sneg``, shared by every reader of the same value),
+    and a modified constant becomes the constant with that sign.  Arguments of
+    exp/log/sqrt/div keep their modifiers (flags of their step format)."""
+    memo = {}
+
+    def plain(y):
+        b, neg, ab = resolve(P, y)
+        if not (neg or ab):
+            return b
+        if P.nodes[b][0] == "const":
+            bits = P.nodes[b][1][0]
+            bits = (bits & ABS) if ab else bits
+            return P.const_bits(bits ^ SIGN if neg else bits)
+        key = (b, neg, ab)
+        if key not in memo:
+            t = P.add("sabs", b) if ab else b
+            memo[key] = P.add("sneg", t) if neg else t
+        return memo[key]
+
+    for x in range(len(P.nodes)):
+        op, a = P.nodes[x]
+        if op in FMA_OPS or op in INT_OP:
+            P.nodes[x] = (op, tuple(plain(y) for y in a))
+
+
+def live_nodes(P: Program, roots) -> list:
+    """The computed nodes the roots depend on (neg/abs folded), sorted."""
+    leaf = ("in", "const")
+    seen, stack = set(), [resolve(P, r)[0] for r in roots]
+    while stack:
+        x = stack.pop()
+        if x in seen:
+            continue
+        seen.add(x)
+        op, a = P.nodes[x]
+        if op in leaf:
+            continue
+        for y in a:
+            stack.append(resolve(P, y)[0])
+    return sorted(x for x in seen if P.nodes[x][0] not in leaf)
+
+
+def roots_of(out: dict) -> list:
+    return list(out["rhs"]) + ([x for _, x in sorted(out["jac"].items())] if "jac" in out else [])
+
+
+def reserved_constants(P: Program, out: dict) -> set:
+    """Constants the program reads from reserved slots: the operands of integer
+    nodes, the minuend of K - b, and constant outputs."""
+    res = set()
+    for x in live_nodes(P, roots_of(out)):
+        op, a = P.nodes[x]
+        if op in INT_OP or op == "sub":
+            for y in (a if op in INT_OP else a[:1]):
+                b = resolve(P, y)[0]
+                if P.nodes[b][0] == "const":
+                    res.add(P.nodes[b][1][0])
+    for r in roots_of(out):
+        b = resolve(P, r)[0]
+        if P.nodes[b][0] == "const":
+            res.add(P.nodes[b][1][0])
+    return res
+
+
 class Schedule:
     def __init__(self, G, steps, slot, nv, outputs, consts):
         self.G = G
@@ -356,7 +451,7 @@ def sink_riders(steps, users, kind, G):
     return [(cls, take, lanes[s]) for s, (cls, take, _) in enumerate(steps) if take or lanes[s]]
 
 
-def schedule(P: Program, out: dict, G: int, jac: bool, limit=None):
+def schedule(P: Program, out: dict, G: int, jac: bool, limit=None, first_scratch=RES_BASE):
     """List-schedule the program into steps of width G and allocate slots.
 
     ``jac``: the program computes the Jacobian too.  Its 225 entries are kept
@@ -364,23 +459,12 @@ def schedule(P: Program, out: dict, G: int, jac: bool, limit=None):
     the iteration matrix's slots serve as scratch); after the program the kernel
     gathers E = -J into the matrix slots from the ``jac`` output table.  Kept
     values therefore live above the matrix slots.  The RHS-only program runs
-    while the matrix holds LU factors, so it never writes the matrix slots."""
+    while the matrix holds LU factors, so it never writes the matrix slots.
+    ``first_scratch``: the first slot above the reserved constants."""
     leaf = ("in", "const")
     jac_roots = [x for _, x in sorted(out["jac"].items())] if jac else []
     roots = list(out["rhs"]) + jac_roots
-    # live compute nodes (neg/abs folded)
-    seen, stack = set(), [resolve(P, r)[0] for r in roots]
-    while stack:
-        x = stack.pop()
-        if x in seen:
-            continue
-        seen.add(x)
-        op, a = P.nodes[x]
-        if op in leaf:
-            continue
-        for y in a:
-            stack.append(resolve(P, y)[0])
-    comp = sorted(x for x in seen if P.nodes[x][0] not in leaf)
+    comp = live_nodes(P, roots)
     args = {x: [resolve(P, a)[0] for a in P.nodes[x][1]] for x in comp}
     cargs = {x: sorted({a for a in args[x] if P.nodes[a][0] not in leaf}) for x in comp}
     users = collections.defaultdict(list)
@@ -425,7 +509,7 @@ def schedule(P: Program, out: dict, G: int, jac: bool, limit=None):
     inputs = [x for x in range(len(P.nodes)) if P.nodes[x][0] == "in"]
     low = list(range(E_SLOTS)) if jac else []  # min-heaps of free slots
     high = []
-    next_slot = Y_BASE + 15
+    next_slot = first_scratch
     release = collections.defaultdict(list)
     for x in inputs:
         slot[x] = Y_BASE + P.nodes[x][1][0]
@@ -460,73 +544,105 @@ def schedule(P: Program, out: dict, G: int, jac: bool, limit=None):
     return Schedule(G, steps, slot, nv, outputs, None), args
 
 
-def encode(P: Program, sch: Schedule, args, cidx: dict, sink: int, one: int, mzero: int):
-    """Per-step, per-lane (main, int) words."""
+def encode(P: Program, sch: Schedule, res: dict) -> list:
+    """Per-step, per-lane (main, integer, literal) words; ``res`` maps the bits of
+    each reserved constant to its slot.  Steps are padded with idle steps (all
+    words zero) to a multiple of ``STEP_ALIGN``, then ``PREFETCH_PAD`` more."""
     G = sch.G
-    # boolean constants (the integers 0 and 1)
-    c_true = cidx[1] | OPF_CONST
-    c_false = cidx[0] | OPF_CONST
+    ZERO, IONE, ONE, MONE, MZERO = (res[b] for b in (0, 1, dbits(1.0), dbits(-1.0), dbits(-0.0)))
+    sink = sch.nv - 1
 
-    def operand(x, neg=False, ab=False):
-        b, n2, a2 = resolve(P, x)
-        # compose the caller's modifiers outside the node's own chain
-        if ab:
-            n2, a2 = False, True
-        if neg:
-            n2 = not n2
-        if P.nodes[b][0] == "const":
-            v = cidx[P.nodes[b][1][0]] | OPF_CONST
-        else:
-            v = sch.slot[b]
-        return v | (OPF_NEG if n2 else 0) | (OPF_ABS if a2 else 0)
+    def const(x):
+        return P.nodes[resolve(P, x)[0]][0] == "const"
 
-    c_one = cidx[one] | OPF_CONST
-    c_mzero = cidx[mzero] | OPF_CONST
+    def cbits(x):  # a constant operand with its modifiers applied
+        b, neg, ab = resolve(P, x)
+        bits = P.nodes[b][1][0]
+        bits = (bits & ABS) if ab else bits
+        return bits ^ SIGN if neg else bits
+
+    def plain(x):  # slot of an operand without modifiers (constants: reserved)
+        b, neg, ab = resolve(P, x)
+        assert not (neg or ab), "operand modifier left on an FMA or integer node"
+        return res[P.nodes[b][1][0]] if P.nodes[b][0] == "const" else sch.slot[b]
+
+    def arg(x):  # slot and modifier flags of an exp/log/sqrt/div argument
+        b, neg, ab = resolve(P, x)
+        return sch.slot[b], (FL_NEG if neg else 0) | (FL_ABS if ab else 0)
+
     words = []
     for cls, take, riders in sch.steps:
+        special = any(P.nodes[x][0] in ("le", "lt", "sneg", "sabs") for x in riders)
+        zfl = (FL_INT if riders else 0) | (FL_SPECIAL if special else 0)
         lanes = []
         for g in range(G):
+            xf = yf = 0
+            L = 0
+            X = Y = Z = ONE
+            dst = sink
             if g < len(take):
                 x = take[g]
                 op, a = P.nodes[x]
+                if op in FMA_OPS:
+                    assert not (const(a[0]) and const(a[1])), "FMA node of two constants"
                 if op == "mul":
-                    p, q, s = operand(a[0]), operand(a[1]), c_mzero
+                    if const(a[0]) or const(a[1]):
+                        v, k = (a[1], a[0]) if const(a[0]) else (a[0], a[1])
+                        X, Y, Z, L = plain(v), ZERO, MZERO, cbits(k)
+                    else:
+                        X, Y, Z = plain(a[0]), plain(a[1]), MZERO
                 elif op == "add":
-                    p, q, s = operand(a[0]), c_one, operand(a[1])
+                    if const(a[0]) or const(a[1]):
+                        v, k = (a[1], a[0]) if const(a[0]) else (a[0], a[1])
+                        X, Y, Z, L = ONE, ZERO, plain(v), cbits(k)
+                    else:
+                        X, Y, Z = plain(a[0]), ONE, plain(a[1])
                 elif op == "sub":
-                    p, q, s = operand(a[0]), c_one, operand(a[1], neg=True)
+                    if const(a[1]):  # a - K = fma(1, -K, a)
+                        X, Y, Z, L = ONE, ZERO, plain(a[0]), cbits(a[1]) ^ SIGN
+                    else:  # a - b = fma(b, -1, a); K - b reads K from its reserved slot
+                        X, Y, Z = plain(a[1]), MONE, plain(a[0])
                 elif op == "div":
-                    p, q, s = operand(a[0]), operand(a[1]), c_one
+                    num, den = a
+                    if const(num):  # K / b: V[Y] ^ L = K, divided by V[X] = b
+                        (X, xf), Y, L, yf = arg(den), ZERO, cbits(num), FL_SWAP
+                    elif const(den):
+                        (X, xf), Y, L = arg(num), ZERO, cbits(den)
+                    else:
+                        (X, xf), (Y, yf) = arg(num), arg(den)
                 else:  # exp, log, sqrt (and their constant-argument forms)
-                    p, q, s = operand(a[0]), c_one, c_one
+                    if const(a[0]):
+                        Y, L = ZERO, cbits(a[0])
+                    else:
+                        Y, yf = arg(a[0])
                 dst = sch.slot[x]
-            else:
-                p = q = s = c_one
-                dst = sink
-            hi = (cls << 60) | ((1 << 63) if riders else 0)
-            has_cmp = any(P.nodes[x][0] in ("le", "lt") for x in riders)
-            main = hi | (dst << 48) | (s << 32) | (q << 16) | p | (OPF_STEP_CMP if has_cmp else 0)
+            main = ((X << 3) | xf) | (((Y << 3) | yf) << 16) | (((Z << 3) | zfl) << 32) | (((dst << 3) | cls) << 48)
+            A, B, C, iop, idst = IONE, ONE, ONE, I_SEL, sink
             if g < len(riders):
                 x = riders[g]
                 op, a = P.nodes[x]
                 iop = INT_OP[op]
                 if op == "and":
-                    ops = [operand(a[0]), operand(a[1]), c_false]
+                    A, B, C = plain(a[0]), plain(a[1]), ZERO
                 elif op == "or":
-                    ops = [operand(a[0]), c_true, operand(a[1])]
+                    A, B, C = plain(a[0]), IONE, plain(a[1])
                 elif op == "not":
-                    ops = [operand(a[0]), c_false, c_true]
+                    A, B, C = plain(a[0]), ZERO, IONE
                 elif op == "sel":
-                    ops = [operand(a[0]), operand(a[1]), operand(a[2])]
-                else:  # le, lt
-                    ops = [operand(a[0]), operand(a[1]), c_true]
+                    A, B, C = plain(a[0]), plain(a[1]), plain(a[2])
+                elif op in ("le", "lt"):
+                    A, B = plain(a[0]), plain(a[1])
+                else:  # sneg, sabs
+                    A = plain(a[0])
+                    iop |= FL_SABS if op == "sabs" else 0
                 idst = sch.slot[x]
-            else:
-                iop, ops, idst = I_SEL, [c_true, c_one, c_one], sink
-            iw = (iop << 60) | (idst << 48) | (ops[2] << 32) | (ops[1] << 16) | ops[0]
-            lanes.append((main, iw))
+            rider = (A << 3) | ((B << 3) << 16) | ((C << 3) << 32) | (((idst << 3) | iop) << 48)
+            lanes.append((main, rider, L))
         words.append(lanes)
-    return words
+    idle = [(0, 0, 0)] * G
+    while len(words) % STEP_ALIGN:
+        words.append(idle)
+    return words + [idle] * PREFETCH_PAD
 
 
 # live-set limit of the list scheduler per G (chosen offline: the smallest slot
@@ -539,55 +655,58 @@ SMEM_BLOCK = 232448
 MAX_WARPS = 16
 
 
-def warps_per_block(G: int, nv: int, nc: int) -> int:
+def warps_per_block(G: int, nv: int) -> int:
     """Warps of the cooperative advance's block: as many as the cells' slot
-    arrays and the constant table fit in one block's shared memory (one block
-    per SM), at most MAX_WARPS."""
-    ncpad = (nc + 1) & ~1
-    cells = (SMEM_BLOCK // 8 - ncpad) // nv
+    arrays fit in one block's shared memory (one block per SM), at most
+    MAX_WARPS."""
+    cells = (SMEM_BLOCK // 8) // nv
     return max(1, min(MAX_WARPS, cells // (32 // G)))
 
 
 def generate(G: int, dag=None, limit="default"):
     """Programs jrhs and rhs for G lanes per cell: a dict with the encoded steps,
-    the output operands, the slot count, the constant table and the warps per
-    block."""
+    the output operands, the slot count, the reserved constants and the warps
+    per block."""
     dag = dag or ir_io.load()
     if limit == "default":
         limit = SCHED_LIMIT.get(G)
-    progs = {}
-    consts = set()
     built = {}
+    pool = {0, 1, dbits(1.0), dbits(-1.0), dbits(-0.0)}
     for kind in ("jrhs", "rhs"):
         P, out = build(dag, kind)
-        sch, args = schedule(P, out, G, jac=(kind == "jrhs"), limit=limit)
-        built[kind] = (P, out, sch, args)
-        for x in range(len(P.nodes)):
-            if P.nodes[x][0] == "const":
-                consts.add(P.nodes[x][1][0])
-    one, mzero = dbits(1.0), dbits(-0.0)
-    consts |= {one, mzero, 0, 1}
-    ctab = sorted(consts)
-    cidx = {b: i for i, b in enumerate(ctab)}
-    if len(ctab) > MAX_SLOTS:
-        raise ValueError("constant table too large")
-    nv = max(b[2].nv for b in built.values())
-    sink = nv - 1
-    for kind, (P, out, sch, args) in built.items():
-        words = encode(P, sch, args, cidx, sink, one, mzero)
+        lower(P)
+        pool |= reserved_constants(P, out)
+        built[kind] = (P, out)
+    # reserved slots: false/+0.0, true, 1, -1, -0 first, then the rest in order
+    fixed = [0, 1, dbits(1.0), dbits(-1.0), dbits(-0.0)]
+    rconst = fixed + sorted(pool - set(fixed))
+    res = {b: RES_BASE + i for i, b in enumerate(rconst)}
+    first = RES_BASE + len(rconst)
+    scheds = {}
+    for kind, (P, out) in built.items():
+        scheds[kind] = schedule(P, out, G, jac=(kind == "jrhs"), limit=limit, first_scratch=first)
+    nv = max(sch.nv for sch, _ in scheds.values())
+    if nv * 8 > 0xfff8:
+        raise ValueError(f"{nv} slots do not fit the 16-bit byte offsets")
+    progs = {}
+    for kind, (P, out) in built.items():
+        sch, _ = scheds[kind]
+        st = stats(sch)
+        sch.nv = nv  # one slot map (and one write sink, the last slot) for both programs
+        words = encode(P, sch, res)
 
         def outop(r, negate=False):
             b, neg, ab = r
             if negate:
                 neg = not neg
-            v = (cidx[P.nodes[b][1][0]] | OPF_CONST) if P.nodes[b][0] == "const" else sch.slot[b]
+            v = res[P.nodes[b][1][0]] if P.nodes[b][0] == "const" else sch.slot[b]
             return v | (OPF_NEG if neg else 0) | (OPF_ABS if ab else 0)
 
         progs[kind] = {"words": words, "rhs_out": [outop(r) for r in sch.outputs["rhs"]],
-                       "nsteps": len(sch.steps), "stats": stats(sch)}
+                       "nsteps": len(words) - PREFETCH_PAD, "stats": st}
         if "jac" in sch.outputs:  # E = -J, entry r * 15 + c
             progs[kind]["jac_out"] = [outop(r, negate=True) for r in sch.outputs["jac"]]
-    return {"G": G, "nv": nv, "consts": ctab, "progs": progs, "warps": warps_per_block(G, nv, len(ctab))}
+    return {"G": G, "nv": nv, "rconst": rconst, "progs": progs, "warps": warps_per_block(G, nv)}
 
 
 def stats(sch: Schedule) -> dict:
@@ -608,24 +727,29 @@ def emit_header(G: int, gen: dict, digest: str) -> str:
         f"namespace wr {{ namespace coop{G} {{",
         f"constexpr int kG = {G};",
         f"constexpr int kNV = {gen['nv']};",
-        f"constexpr int kNC = {len(gen['consts'])};",
+        f"constexpr int kNR = {len(gen['rconst'])};  // reserved constant slots from {RES_BASE}",
         f"constexpr int kWarps = {gen['warps']};  // warps per block: the slot arrays that fit in shared memory",
     ]
     for kind, pr in gen["progs"].items():
         st = pr["stats"]
         lines.append(f"constexpr int k{kind.upper()}Steps = {pr['nsteps']};  // {st['by_class']}, "
-                     f"{st['fp64_slots']:.0f} FP64 issue slots")
+                     f"{st['fp64_slots']:.0f} FP64 issue slots, {st['steps']} steps before padding")
     lines.append("")
-    lines.append("static __device__ const uint64_t kConst[kNC] = {")
-    cs = gen["consts"]
+    lines.append("static __device__ const uint64_t kVConst[kNR] = {")
+    cs = gen["rconst"]
     for i in range(0, len(cs), 4):
         lines.append("    " + ", ".join(f"0x{b:016x}ULL" for b in cs[i:i + 4]) + ",")
     lines.append("};")
     for kind, pr in gen["progs"].items():
         K = kind.upper()
-        lines.append(f"static __device__ const ulonglong2 k{K}Prog[k{K}Steps * kG] = {{")
+        n = f"(k{K}Steps + {PREFETCH_PAD}) * kG"
+        lines.append(f"static __device__ const ulonglong2 k{K}Prog[{n}] = {{")
         for lanes in pr["words"]:
-            lines.append("    " + ", ".join(f"{{0x{m:x}ULL, 0x{i:x}ULL}}" for m, i in lanes) + ",")
+            lines.append("    " + ", ".join(f"{{0x{m:x}ULL, 0x{i:x}ULL}}" for m, i, _ in lanes) + ",")
+        lines.append("};")
+        lines.append(f"static __device__ const uint64_t k{K}Lit[{n}] = {{")
+        for lanes in pr["words"]:
+            lines.append("    " + ", ".join(f"0x{l:x}ULL" for _, _, l in lanes) + ",")
         lines.append("};")
         lines.append(f"static __device__ const uint16_t k{K}Out[15] = {{" +
                      ", ".join(str(v) for v in pr["rhs_out"]) + "};")
@@ -660,4 +784,4 @@ if __name__ == "__main__":
     d = ir_io.load()
     for G in LANES_PER_CELL:
         g = generate(G, d)
-        print(G, g["nv"], len(g["consts"]), {k: v["stats"] for k, v in g["progs"].items()})
+        print(G, g["nv"], len(g["rconst"]), g["warps"], {k: v["stats"] for k, v in g["progs"].items()})
