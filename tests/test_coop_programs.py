@@ -77,7 +77,7 @@ def ble(a, b):
 
 def run(words, V, nres, oracle, written=None):
     sink = len(V) - 1
-    reserved = set(range(coop.RES_BASE, coop.RES_BASE + nres))
+    reserved = set(range(coop.RES_BASE, coop.RES_BASE + nres))  # constants and transcendentals of constants
     for lanes in words:
         reads, writes, results = set(), set(), []
         for mw, iw, lit in lanes:
@@ -172,10 +172,13 @@ def test_programs_equal_oracle(programs, oracle_port, G):
             V = [0x7ff4000000000000] * gen["nv"]  # signalling-NaN garbage: every read slot must be written
             for i, b in enumerate(gen["rconst"]):
                 V[coop.RES_BASE + i] = b
+            fn = {C_EXP: oracle_port.exp, C_LOG: oracle_port.log, C_SQRT: math.sqrt}
+            for j, (cls, b) in enumerate(gen["rfun"]):  # the kernel's per-launch evaluation
+                V[coop.RES_BASE + nres + j] = u(fn[cls](d(b)))
             for k in range(15):
                 V[coop.Y_BASE + k] = u(y[k])
             written = set()
-            run(pr["words"], V, nres, oracle_port, written)
+            run(pr["words"], V, nres + len(gen["rfun"]), oracle_port, written)
             f = np.array([d(fetch(V, o)) for o in pr["rhs_out"]])
             assert same(f, f_o), (G, kind)
             assert all((o & 0xfff) >= coop.E_SLOTS for o in pr["rhs_out"])

@@ -17,6 +17,7 @@ namespace cp = WR_CAT(coop, WR_COOP_G);
 struct Tab {
     static constexpr int kNV = cp::kNV;
     static constexpr int kNR = cp::kNR;
+    static constexpr int kNF = cp::kNF;
     static constexpr int kJSteps = cp::kJRHSSteps;
     static constexpr int kRSteps = cp::kRHSSteps;
     static __device__ __forceinline__ const ulonglong2* jprog() { return cp::kJRHSProg; }
@@ -27,9 +28,10 @@ struct Tab {
     static __device__ __forceinline__ const uint16_t* jac() { return cp::kJRHSJac; }
     static __device__ __forceinline__ const uint16_t* rout() { return cp::kRHSOut; }
     static __device__ __forceinline__ const uint64_t* vconst() { return cp::kVConst; }
+    static __device__ __forceinline__ const ulonglong2* vfun() { return cp::kVFun; }
 };
 static_assert(Tab::kJSteps % 4 == 0 && Tab::kRSteps % 4 == 0, "programs are padded to groups of four steps");
-static_assert(coop::kRes + Tab::kNR <= Tab::kNV, "reserved constants lie inside the slot array");
+static_assert(coop::kRes + Tab::kNR + Tab::kNF <= Tab::kNV, "reserved constants lie inside the slot array");
 
 constexpr int kG = WR_COOP_G;
 constexpr int kW = cp::kWarps;

@@ -59,7 +59,7 @@ enum : uint32_t {
 };
 constexpr int kE = 0;        // iteration matrix slots [0, 225)
 constexpr int kY = 225;      // program inputs y[0..14]
-constexpr int kRes = 240;    // reserved constants [240, 240 + Tab::kNR)
+constexpr int kRes = 240;    // reserved constants [240, 240 + Tab::kNR + Tab::kNF)
 constexpr uint32_t kOff = 0xfff8u;
 constexpr uint64_t kSign = 0x8000000000000000ULL;
 constexpr uint64_t kAbs = 0x7fffffffffffffffULL;
@@ -209,10 +209,18 @@ __device__ __noinline__ void run_prog(const ulonglong2* __restrict__ prog, const
 }
 
 // the reserved constants of the programs into the group's slot array (once per
-// launch: no program writes them)
-template <int G, class Tab>
+// launch: no program writes them), then the exp/log/sqrt of constants, evaluated
+// here with the kernel's own functions so that they are the bits a program step
+// would compute
+template <class M, int G, class Tab>
 __device__ __forceinline__ void init_reserved(uint64_t* V, int gl, unsigned gmask) {
     for (int i = gl; i < Tab::kNR; i += G) V[kRes + i] = Tab::vconst()[i];
+    for (int i = gl; i < Tab::kNF; i += G) {
+        const ulonglong2 f = Tab::vfun()[i];
+        const double a = dbl(f.y);
+        const double r = f.x == C_EXP ? StepMath<M>::exp(a) : f.x == C_LOG ? StepMath<M>::log(a) : StepMath<M>::sqrt(a);
+        V[kRes + Tab::kNR + i] = bits(r);
+    }
     __syncwarp(gmask);
 }
 
@@ -370,8 +378,8 @@ __device__ __forceinline__ void gather_matrix(uint64_t* V, const uint16_t* jac, 
 
 // Generated tables of one G, supplied by the translation unit that includes the
 // generated header (one unit per G keeps the large initialisers apart).
-//   Tab::kNV, Tab::kNR, Tab::kJSteps, Tab::kRSteps and device accessors
-//   jprog(), jlit(), rprog(), rlit(), jout(), jac(), rout(), vconst().
+//   Tab::kNV, Tab::kNR, Tab::kNF, Tab::kJSteps, Tab::kRSteps and device accessors
+//   jprog(), jlit(), rprog(), rlit(), jout(), jac(), rout(), vconst(), vfun().
 
 }  // namespace coop
 
@@ -390,7 +398,7 @@ __global__ void __launch_bounds__(W * 32, 1) k_advance_coop(DevState s, StepCtl*
     const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (slot * G));
     uint64_t* V = sm + static_cast<size_t>((threadIdx.x >> 5) * SLOTS + slot) * Tab::kNV;
     double* E = reinterpret_cast<double*>(V + kE);
-    init_reserved<G, Tab>(V, gl, gmask);
+    init_reserved<M, G, Tab>(V, gl, gmask);
     const int n = s.n;
     const unsigned int queued = ctl->queued;
 
@@ -648,7 +656,7 @@ __global__ void k_diag_coop_network(int n, const double* __restrict__ y, double*
     if (cell >= n) return;
     uint64_t* V = sm + static_cast<size_t>(warp * SLOTS + slot) * Tab::kNV;
     const double* E = reinterpret_cast<const double*>(V + kE);
-    init_reserved<G, Tab>(V, gl, gmask);
+    init_reserved<M, G, Tab>(V, gl, gmask);
     double yy[K], out[K];
 #pragma unroll
     for (int t = 0; t < K; ++t) {

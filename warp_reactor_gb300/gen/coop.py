@@ -85,6 +85,7 @@ from __future__ import annotations
 
 import collections
 import os
+import random
 import struct
 
 from . import ir_io
@@ -125,6 +126,11 @@ STEP_ALIGN = 4
 PREFETCH_PAD = 4
 SIGN = 1 << 63
 ABS = SIGN - 1
+# leaves of a program: inputs, constants, and transcendentals of constants
+# ("dconst": evaluated once per launch on the device, with the kernel's own
+# exp/log/sqrt, into reserved slots)
+LEAF = ("in", "const", "dconst")
+TRANSCENDENTAL = {"exp": C_EXP, "cexp": C_EXP, "log": C_LOG, "clog": C_LOG, "sqrt": C_SQRT, "csqrt": C_SQRT}
 
 FLOOR = 1.0e-100  # reproducer.cpp:231
 # species masses, reproducer.cpp:233-248 (the literals of wr_physics.cuh)
@@ -307,8 +313,20 @@ def lower(P: Program) -> None:
     format reads plain slots: a negated or absolute operand becomes an integer
     sign node (``sabs`` then ``sneg``, shared by every reader of the same value),
     and a modified constant becomes the constant with that sign.  Arguments of
-    exp/log/sqrt/div keep their modifiers (flags of their step format)."""
+    exp/log/sqrt/div keep their modifiers (flags of their step format).
+
+    An exp, log or sqrt of a constant becomes a ``dconst`` leaf (class, argument
+    bits): the kernel evaluates it once per launch with its own math functions,
+    so every program run reads the same bits it would have computed."""
     memo = {}
+    for x in range(len(P.nodes)):
+        op, a = P.nodes[x]
+        if op in TRANSCENDENTAL:
+            b, neg, ab = resolve(P, a[0])
+            if P.nodes[b][0] == "const":
+                bits = P.nodes[b][1][0]
+                bits = (bits & ABS) if ab else bits
+                P.nodes[x] = ("dconst", (TRANSCENDENTAL[op], bits ^ SIGN if neg else bits))
 
     def plain(y):
         b, neg, ab = resolve(P, y)
@@ -330,9 +348,10 @@ def lower(P: Program) -> None:
             P.nodes[x] = (op, tuple(plain(y) for y in a))
 
 
-def live_nodes(P: Program, roots) -> list:
-    """The computed nodes the roots depend on (neg/abs folded), sorted."""
-    leaf = ("in", "const")
+def live_nodes(P: Program, roots, leaves=False) -> list:
+    """The computed nodes the roots depend on (neg/abs folded), sorted; with
+    ``leaves``, the leaves they read too."""
+    leaf = LEAF
     seen, stack = set(), [resolve(P, r)[0] for r in roots]
     while stack:
         x = stack.pop()
@@ -344,11 +363,16 @@ def live_nodes(P: Program, roots) -> list:
             continue
         for y in a:
             stack.append(resolve(P, y)[0])
-    return sorted(x for x in seen if P.nodes[x][0] not in leaf)
+    return sorted(x for x in seen if leaves or P.nodes[x][0] not in leaf)
 
 
 def roots_of(out: dict) -> list:
     return list(out["rhs"]) + ([x for _, x in sorted(out["jac"].items())] if "jac" in out else [])
+
+
+def device_constants(P: Program, out: dict) -> set:
+    """The (class, argument bits) of the program's transcendentals of constants."""
+    return {P.nodes[x][1] for x in live_nodes(P, roots_of(out), leaves=True) if P.nodes[x][0] == "dconst"}
 
 
 def reserved_constants(P: Program, out: dict) -> set:
@@ -379,10 +403,15 @@ class Schedule:
         self.consts = consts
 
 
-def list_schedule(comp, args, users, kind, prio, G, limit=None):
+def list_schedule(comp, args, users, kind, prio, G, limit=None, hold=None):
     """Steps of width G: each step takes up to G ready nodes of one main class
     (highest priority first; a full step is preferred) and up to G ready integer
     nodes.  ``args``/``users`` give the dependences in the direction scheduled.
+
+    ``hold``: a partial exp/log/sqrt step costs as many FP64 issue slots as a full
+    one, so while an FMA or division step can be filled instead, a transcendental
+    class is taken only if its most critical ready node leads theirs by more than
+    ``hold`` (None: no such rule).
 
     ``limit``: once that many computed values are live (computed, with users not
     yet scheduled), ready nodes are taken by their effect on the live set first
@@ -405,6 +434,9 @@ def list_schedule(comp, args, users, kind, prio, G, limit=None):
             return ((1 if users[x] else 0) - freed, -prio[x])
         return (0, -prio[x])
 
+    def top(c):
+        return max(prio[x] for x in ready[c])
+
     while left:
         rl = sorted(ready["int"], key=key)
         riders, ready["int"] = rl[:G], rl[G:]
@@ -413,7 +445,11 @@ def list_schedule(comp, args, users, kind, prio, G, limit=None):
         if cand:
             full = [c for c in cand if len(ready[c]) >= G]
             pool = full if full else cand
-            cls = max(pool, key=lambda c: (max(prio[x] for x in ready[c]), len(ready[c])))
+            cheap = [c for c in cand if c in (C_FMA, C_DIV)]
+            if hold is not None and not full and cheap:
+                lead = max(top(c) for c in cheap)
+                pool = cheap + [c for c in cand if c not in cheap and top(c) > lead + hold]
+            cls = max(pool, key=lambda c: (top(c), len(ready[c])))
             rl = sorted(ready[cls], key=key)
             take, ready[cls] = rl[:G], rl[G:]
         steps.append((cls, take, riders))
@@ -451,7 +487,7 @@ def sink_riders(steps, users, kind, G):
     return [(cls, take, lanes[s]) for s, (cls, take, _) in enumerate(steps) if take or lanes[s]]
 
 
-def schedule(P: Program, out: dict, G: int, jac: bool, limit=None, first_scratch=RES_BASE):
+def schedule(P: Program, out: dict, G: int, jac: bool, limit=None, first_scratch=RES_BASE, tune=None):
     """List-schedule the program into steps of width G and allocate slots.
 
     ``jac``: the program computes the Jacobian too.  Its 225 entries are kept
@@ -460,8 +496,11 @@ def schedule(P: Program, out: dict, G: int, jac: bool, limit=None, first_scratch
     gathers E = -J into the matrix slots from the ``jac`` output table.  Kept
     values therefore live above the matrix slots.  The RHS-only program runs
     while the matrix holds LU factors, so it never writes the matrix slots.
-    ``first_scratch``: the first slot above the reserved constants."""
-    leaf = ("in", "const")
+    ``first_scratch``: the first slot above the reserved constants.  ``tune``:
+    (latency weight of exp/log/sqrt, ``hold`` of the list scheduler, seed of a
+    tie-breaking perturbation of the priorities, below 1e-3; 0 for none) -- the
+    schedule is a heuristic, and these pick among equally valid ones."""
+    leaf = LEAF
     jac_roots = [x for _, x in sorted(out["jac"].items())] if jac else []
     roots = list(out["rhs"]) + jac_roots
     comp = live_nodes(P, roots)
@@ -484,10 +523,15 @@ def schedule(P: Program, out: dict, G: int, jac: bool, limit=None, first_scratch
             if pend[u] == 0:
                 order.append(u)
     assert len(order) == len(comp), "the program has a cycle"
+    lat_t, hold, seed = tune or (LATENCY[C_EXP], None, 0)
+    lat = dict(LATENCY)
+    lat.update({C_EXP: lat_t, C_LOG: lat_t, C_SQRT: max(1.0, lat_t - 1.0)})
+    rng = random.Random(seed)
     prio = {}
     for x in reversed(order):
-        prio[x] = LATENCY[kind(x)] + max((prio[u] for u in users[x]), default=0.0)
-    steps = sink_riders(list_schedule(comp, cargs, users, kind, prio, G, limit), users, kind, G)
+        prio[x] = lat[kind(x)] + max((prio[u] for u in users[x]), default=0.0)
+        prio[x] += rng.random() * 1e-3 if seed else 0.0
+    steps = sink_riders(list_schedule(comp, cargs, users, kind, prio, G, limit, hold), users, kind, G)
     done_at = {}
     for s, (cls, take, riders) in enumerate(steps):
         for x in take + riders:
@@ -546,7 +590,8 @@ def schedule(P: Program, out: dict, G: int, jac: bool, limit=None, first_scratch
 
 def encode(P: Program, sch: Schedule, res: dict) -> list:
     """Per-step, per-lane (main, integer, literal) words; ``res`` maps the bits of
-    each reserved constant to its slot.  Steps are padded with idle steps (all
+    each reserved constant, and the (class, argument bits) of each transcendental
+    of a constant, to its slot.  Steps are padded with idle steps (all
     words zero) to a multiple of ``STEP_ALIGN``, then ``PREFETCH_PAD`` more."""
     G = sch.G
     ZERO, IONE, ONE, MONE, MZERO = (res[b] for b in (0, 1, dbits(1.0), dbits(-1.0), dbits(-0.0)))
@@ -561,14 +606,18 @@ def encode(P: Program, sch: Schedule, res: dict) -> list:
         bits = (bits & ABS) if ab else bits
         return bits ^ SIGN if neg else bits
 
+    def slot_of(b):
+        op = P.nodes[b][0]
+        return res[P.nodes[b][1][0]] if op == "const" else res[P.nodes[b][1]] if op == "dconst" else sch.slot[b]
+
     def plain(x):  # slot of an operand without modifiers (constants: reserved)
         b, neg, ab = resolve(P, x)
         assert not (neg or ab), "operand modifier left on an FMA or integer node"
-        return res[P.nodes[b][1][0]] if P.nodes[b][0] == "const" else sch.slot[b]
+        return slot_of(b)
 
     def arg(x):  # slot and modifier flags of an exp/log/sqrt/div argument
         b, neg, ab = resolve(P, x)
-        return sch.slot[b], (FL_NEG if neg else 0) | (FL_ABS if ab else 0)
+        return slot_of(b), (FL_NEG if neg else 0) | (FL_ABS if ab else 0)
 
     words = []
     for cls, take, riders in sch.steps:
@@ -648,6 +697,14 @@ def encode(P: Program, sch: Schedule, res: dict) -> list:
 # live-set limit of the list scheduler per G (chosen offline: the smallest slot
 # count among limits that do not add FP64 issue slots)
 SCHED_LIMIT = {8: 400, 16: 650, 32: None}
+# scheduler tuning per G and program: (schedule()'s ``tune``, live-set limit),
+# chosen offline by a seeded random search for the fewest FP64 issue slots of the
+# program whose slot count keeps the block's warps (16 lanes: 16 warps, <= 907
+# slots; 8 lanes: 9 warps, <= 807 slots)
+SCHED_TUNE = {
+    16: {"jrhs": ((6.0, 3.0, 588627), 550), "rhs": ((1.5, None, 405133), 550)},
+    8: {"jrhs": ((2.0, 0.0, 509381), 400), "rhs": ((2.0, 1.0, 795782), 500)},
+}
 # shared memory of one block (227 KiB) and the warps per block the slot arrays
 # allow, at most 16: at 16 lanes per cell (728 slots) 16 warps ran a 64^3 collapse
 # in 32.5 s on GB300, 17 warps in 34.3 s and 19 warps (register-limited) in 33.3 s
@@ -663,28 +720,36 @@ def warps_per_block(G: int, nv: int) -> int:
     return max(1, min(MAX_WARPS, cells // (32 // G)))
 
 
-def generate(G: int, dag=None, limit="default"):
+def generate(G: int, dag=None, limit="default", tune="default"):
     """Programs jrhs and rhs for G lanes per cell: a dict with the encoded steps,
     the output operands, the slot count, the reserved constants and the warps
     per block."""
     dag = dag or ir_io.load()
     if limit == "default":
         limit = SCHED_LIMIT.get(G)
+    if tune == "default":
+        tune = SCHED_TUNE.get(G)
     built = {}
     pool = {0, 1, dbits(1.0), dbits(-1.0), dbits(-0.0)}
+    funs = set()
     for kind in ("jrhs", "rhs"):
         P, out = build(dag, kind)
         lower(P)
         pool |= reserved_constants(P, out)
+        funs |= device_constants(P, out)
         built[kind] = (P, out)
-    # reserved slots: false/+0.0, true, 1, -1, -0 first, then the rest in order
+    # reserved slots: false/+0.0, true, 1, -1, -0 first, then the rest in order,
+    # then the transcendentals of constants
     fixed = [0, 1, dbits(1.0), dbits(-1.0), dbits(-0.0)]
     rconst = fixed + sorted(pool - set(fixed))
+    rfun = sorted(funs)
     res = {b: RES_BASE + i for i, b in enumerate(rconst)}
-    first = RES_BASE + len(rconst)
+    res.update({f: RES_BASE + len(rconst) + j for j, f in enumerate(rfun)})
+    first = RES_BASE + len(rconst) + len(rfun)
     scheds = {}
     for kind, (P, out) in built.items():
-        scheds[kind] = schedule(P, out, G, jac=(kind == "jrhs"), limit=limit, first_scratch=first)
+        t, lim = (tune or {}).get(kind, (None, limit))
+        scheds[kind] = schedule(P, out, G, jac=(kind == "jrhs"), limit=lim, first_scratch=first, tune=t)
     nv = max(sch.nv for sch, _ in scheds.values())
     if nv * 8 > 0xfff8:
         raise ValueError(f"{nv} slots do not fit the 16-bit byte offsets")
@@ -699,14 +764,15 @@ def generate(G: int, dag=None, limit="default"):
             b, neg, ab = r
             if negate:
                 neg = not neg
-            v = res[P.nodes[b][1][0]] if P.nodes[b][0] == "const" else sch.slot[b]
+            op = P.nodes[b][0]
+            v = res[P.nodes[b][1][0]] if op == "const" else res[P.nodes[b][1]] if op == "dconst" else sch.slot[b]
             return v | (OPF_NEG if neg else 0) | (OPF_ABS if ab else 0)
 
         progs[kind] = {"words": words, "rhs_out": [outop(r) for r in sch.outputs["rhs"]],
                        "nsteps": len(words) - PREFETCH_PAD, "stats": st}
         if "jac" in sch.outputs:  # E = -J, entry r * 15 + c
             progs[kind]["jac_out"] = [outop(r, negate=True) for r in sch.outputs["jac"]]
-    return {"G": G, "nv": nv, "rconst": rconst, "progs": progs, "warps": warps_per_block(G, nv)}
+    return {"G": G, "nv": nv, "rconst": rconst, "rfun": rfun, "progs": progs, "warps": warps_per_block(G, nv)}
 
 
 def stats(sch: Schedule) -> dict:
@@ -728,6 +794,7 @@ def emit_header(G: int, gen: dict, digest: str) -> str:
         f"constexpr int kG = {G};",
         f"constexpr int kNV = {gen['nv']};",
         f"constexpr int kNR = {len(gen['rconst'])};  // reserved constant slots from {RES_BASE}",
+        f"constexpr int kNF = {len(gen['rfun'])};  // then the transcendentals of constants",
         f"constexpr int kWarps = {gen['warps']};  // warps per block: the slot arrays that fit in shared memory",
     ]
     for kind, pr in gen["progs"].items():
@@ -739,6 +806,11 @@ def emit_header(G: int, gen: dict, digest: str) -> str:
     cs = gen["rconst"]
     for i in range(0, len(cs), 4):
         lines.append("    " + ", ".join(f"0x{b:016x}ULL" for b in cs[i:i + 4]) + ",")
+    lines.append("};")
+    lines.append("// (class, argument bits): exp (2), log (3) or sqrt (4) of a constant")
+    lines.append(f"static __device__ const ulonglong2 kVFun[{max(1, len(gen['rfun']))}] = {{")
+    for c, b in gen["rfun"] or [(0, 0)]:
+        lines.append(f"    {{{c}ULL, 0x{b:016x}ULL}},")
     lines.append("};")
     for kind, pr in gen["progs"].items():
         K = kind.upper()
