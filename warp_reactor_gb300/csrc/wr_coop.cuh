@@ -303,17 +303,32 @@ __device__ __forceinline__ int lu_coop(double* E, int gl, unsigned gmask, uint64
 // component c of a vector distributed over the group: lane c % G, register c / G
 // (c is uniform over the group; the register is picked by a select, so the
 // array stays in registers)
-template <int G, int K>
-__device__ __forceinline__ double get(const double (&x)[K], int c, unsigned gmask) {
-    double v = x[0];
+template <int G, int K, class T>
+__device__ __forceinline__ T get(const T (&x)[K], int c, unsigned gmask) {
+    T v = x[0];
 #pragma unroll
     for (int t = 1; t < K; ++t) v = (c / G == t) ? x[t] : v;
     return __shfl_sync(gmask, v, c % G, G);
 }
 
-// lu_solve<15> (reproducer.cpp:154-181) with x distributed over the group
+// the reciprocals of the factorisation's diagonal for the back substitutions
+// (wr_div_recip of U(c, c), distributed like a vector): the three stage solves
+// of an attempt divide by the same 15 pivots
 template <int G, int K>
-__device__ __forceinline__ void solve_coop(const double* LU, uint64_t ip, double (&x)[K], int gl, unsigned gmask) {
+__device__ __forceinline__ void diag_recips(const double* LU, uint64_t (&rY)[K], int gl) {
+#pragma unroll
+    for (int t = 0; t < K; ++t) {
+        const int c = gl + t * G;
+        rY[t] = c < NEQ ? wr_div_recip(LU[c * NEQ + c]) : 0;
+    }
+}
+
+// lu_solve<15> (reproducer.cpp:154-181) with x distributed over the group; the
+// back substitution's quotients use the pivots' precomputed reciprocals (the same
+// IEEE quotients as a division)
+template <int G, int K>
+__device__ __forceinline__ void solve_coop(const double* LU, uint64_t ip, const uint64_t (&rY)[K], double (&x)[K],
+                                           int gl, unsigned gmask) {
 #pragma unroll 1
     for (int k = 0; k < NEQ - 1; ++k) {
         const int p = static_cast<int>((ip >> (4 * k)) & 15);
@@ -335,7 +350,8 @@ __device__ __forceinline__ void solve_coop(const double* LU, uint64_t ip, double
     }
 #pragma unroll 1
     for (int k = NEQ - 1; k >= 0; --k) {
-        const double q = ddiv(get<G, K>(x, k, gmask), LU[k * NEQ + k]);
+        const uint64_t yk = get<G, K>(rY, k, gmask);
+        const double q = ddiv_recip(get<G, K>(x, k, gmask), LU[k * NEQ + k], yk);
         const double tk = -q;
 #pragma unroll
         for (int t = 0; t < K; ++t) {
@@ -530,9 +546,11 @@ __global__ void __launch_bounds__(W * 32, 1) k_advance_coop(DevState s, StepCtl*
             continue;
         }
         L.n_decomp += 1;
+        uint64_t rY[K];
+        diag_recips<G, K>(E, rY, gl);
 #pragma unroll
         for (int t = 0; t < K; ++t) ak1[t] = f0[t];
-        solve_coop<G, K>(E, ip, ak1, gl, gmask);
+        solve_coop<G, K>(E, ip, rY, ak1, gl, gmask);
         // stage 2
         {
             double yn[K];
@@ -549,7 +567,7 @@ __global__ void __launch_bounds__(W * 32, 1) k_advance_coop(DevState s, StepCtl*
             load_outputs<G, K>(V, Tab::rout(), dy, gl);
 #pragma unroll
             for (int t = 0; t < K; ++t) w[t] += dy[t];
-            solve_coop<G, K>(E, ip, w, gl, gmask);
+            solve_coop<G, K>(E, ip, rY, w, gl, gmask);
 #pragma unroll
             for (int t = 0; t < K; ++t) ak2[t] = w[t];
         }
@@ -569,7 +587,7 @@ __global__ void __launch_bounds__(W * 32, 1) k_advance_coop(DevState s, StepCtl*
             load_outputs<G, K>(V, Tab::rout(), dy, gl);
 #pragma unroll
             for (int t = 0; t < K; ++t) w[t] += dy[t];
-            solve_coop<G, K>(E, ip, w, gl, gmask);
+            solve_coop<G, K>(E, ip, rY, w, gl, gmask);
         }
         // w = k3: candidate and error estimate, reproducer.cpp:7299-7304
         double ynew[K], sq[K];
@@ -709,7 +727,11 @@ __global__ void k_diag_coop_lu(int n, const double* __restrict__ A, const double
         const int c = gl + t * G;
         v[t] = c < NEQ ? b[static_cast<size_t>(cell) * NEQ + c] : 0.0;
     }
-    if (inf == 0) solve_coop<G, K>(E, ip, v, gl, gmask);
+    if (inf == 0) {
+        uint64_t rY[K];
+        diag_recips<G, K>(E, rY, gl);
+        solve_coop<G, K>(E, ip, rY, v, gl, gmask);
+    }
     __syncwarp(gmask);
     for (int i = gl; i < NEQ * NEQ; i += G) LU[static_cast<size_t>(cell) * NEQ * NEQ + i] = E[i];
 #pragma unroll

@@ -146,18 +146,17 @@ WR_MHD double wr_fixed_to_double(int64_t hi, uint64_t lo, int q) {
 // round-to-nearest-even.
 // Everything else (zeros, subnormals, inf/NaN, overflow/underflow) uses a / b.
 // On GB300 this keeps divisions off the FP64 pipe (a native double division
-// issues about eight FP64 instructions).
-WR_MHD double wr_div_int(double a, double b) {
-    const uint64_t ua = wr_bits(a), ub = wr_bits(b);
-    const uint32_t ea = static_cast<uint32_t>(ua >> 52) & 0x7ff;
-    const uint32_t eb = static_cast<uint32_t>(ub >> 52) & 0x7ff;
-    if (ea - 1u >= 2046u || eb - 1u >= 2046u) return a / b;
-    const uint64_t ma = (ua & 0x000fffffffffffffULL) | 0x0010000000000000ULL;
+// issues about eight FP64 instructions).  wr_div_int (below) is
+// wr_div_finish(a, b, wr_div_recip(b)).
+
+// The divisor's part of wr_div_int: Y ~ 1/b_m in Q63 (b_m = b's significand in
+// [1, 2)) from a float seed and two fixed-point Newton steps.  Any value for a
+// zero, subnormal, infinite or NaN b (wr_div_finish then divides by a / b).  A
+// quotient needs only wr_div_finish with this Y, so several divisions by one b
+// share it.
+WR_MHD uint64_t wr_div_recip(double b) {
+    const uint64_t ub = wr_bits(b);
     const uint64_t mb = (ub & 0x000fffffffffffffULL) | 0x0010000000000000ULL;
-    const int adj = ma < mb ? 1 : 0;
-    const int be = static_cast<int>(ea) - static_cast<int>(eb) - adj + 1023;
-    if (be < 1 || be > 2046) return a / b;
-    // y ~ 1/b_m in Q63, b_m = mb * 2^-52 in [1, 2)
     const float bf = static_cast<float>(static_cast<uint32_t>(mb >> 29));  // exact, 24 bits
 #if defined(__CUDA_ARCH__)
     const float rf = __frcp_rn(bf);
@@ -172,7 +171,22 @@ WR_MHD double wr_div_int(double a, double b) {
         const uint64_t c = e >= 0 ? wr_umulhi(Y, static_cast<uint64_t>(e)) : 0 - wr_umulhi(Y, static_cast<uint64_t>(-e));
         Y += c << 3;
     }
-    // Q ~ floor(ma * 2^(53+adj) / mb), exact remainder R
+    return Y;
+}
+
+// a / b given Y = wr_div_recip(b): a 54-bit quotient Q ~ floor(a_m * 2^(53+adj) /
+// b_m), its exact remainder, at most two corrections each way, round to nearest
+// even.  Operands or quotients outside the normal range divide by a / b.
+WR_MHD double wr_div_finish(double a, double b, uint64_t Y) {
+    const uint64_t ua = wr_bits(a), ub = wr_bits(b);
+    const uint32_t ea = static_cast<uint32_t>(ua >> 52) & 0x7ff;
+    const uint32_t eb = static_cast<uint32_t>(ub >> 52) & 0x7ff;
+    if (ea - 1u >= 2046u || eb - 1u >= 2046u) return a / b;
+    const uint64_t ma = (ua & 0x000fffffffffffffULL) | 0x0010000000000000ULL;
+    const uint64_t mb = (ub & 0x000fffffffffffffULL) | 0x0010000000000000ULL;
+    const int adj = ma < mb ? 1 : 0;
+    const int be = static_cast<int>(ea) - static_cast<int>(eb) - adj + 1023;
+    if (be < 1 || be > 2046) return a / b;
     uint64_t Q = wr_umulhi(ma << (2 + adj), Y);
     int64_t R = static_cast<int64_t>((ma << (53 + adj)) - Q * mb);
     const int64_t smb = static_cast<int64_t>(mb);
@@ -192,6 +206,8 @@ WR_MHD double wr_div_int(double a, double b) {
     return wr_from_bits(((ua ^ ub) & 0x8000000000000000ULL) | (static_cast<uint64_t>(e2) << 52) |
                         (mant & 0x000fffffffffffffULL));
 }
+
+WR_MHD double wr_div_int(double a, double b) { return wr_div_finish(a, b, wr_div_recip(b)); }
 
 WR_MHD double wr_exp(double x) {
     const uint64_t u = wr_bits(x);

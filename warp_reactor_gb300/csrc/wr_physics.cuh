@@ -18,6 +18,9 @@ namespace wr {
 // (wr_div_int), one shared out-of-line copy.  Bit-identical to a / b.
 static __device__ __noinline__ double wr_div_call(double a, double b) { return wr_div_int(a, b); }
 __device__ __forceinline__ double ddiv(double a, double b) { return wr_div_call(a, b); }
+// a / b with b's reciprocal Y = wr_div_recip(b) already computed (several
+// quotients by one divisor): the same bits as ddiv(a, b)
+static __device__ __noinline__ double ddiv_recip(double a, double b, uint64_t Y) { return wr_div_finish(a, b, Y); }
 
 constexpr int NS = 14;
 constexpr int NEQ = 15;

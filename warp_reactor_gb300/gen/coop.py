@@ -411,7 +411,7 @@ def list_schedule(comp, args, users, kind, prio, G, limit=None, hold=None):
     ``hold``: a partial exp/log/sqrt step costs as many FP64 issue slots as a full
     one, so while an FMA or division step can be filled instead, a transcendental
     class is taken only if its most critical ready node leads theirs by more than
-    ``hold`` (None: no such rule).
+    ``hold`` (a number, or one per class; None: no such rule).
 
     ``limit``: once that many computed values are live (computed, with users not
     yet scheduled), ready nodes are taken by their effect on the live set first
@@ -448,7 +448,8 @@ def list_schedule(comp, args, users, kind, prio, G, limit=None, hold=None):
             cheap = [c for c in cand if c in (C_FMA, C_DIV)]
             if hold is not None and not full and cheap:
                 lead = max(top(c) for c in cheap)
-                pool = cheap + [c for c in cand if c not in cheap and top(c) > lead + hold]
+                hc = hold if isinstance(hold, dict) else {c: hold for c in mains}
+                pool = cheap + [c for c in cand if c not in cheap and top(c) > lead + hc.get(c, 0.0)]
             cls = max(pool, key=lambda c: (top(c), len(ready[c])))
             rl = sorted(ready[cls], key=key)
             take, ready[cls] = rl[:G], rl[G:]
@@ -498,8 +499,9 @@ def schedule(P: Program, out: dict, G: int, jac: bool, limit=None, first_scratch
     while the matrix holds LU factors, so it never writes the matrix slots.
     ``first_scratch``: the first slot above the reserved constants.  ``tune``:
     (latency weight of exp/log/sqrt, ``hold`` of the list scheduler, seed of a
-    tie-breaking perturbation of the priorities, below 1e-3; 0 for none) -- the
-    schedule is a heuristic, and these pick among equally valid ones."""
+    random perturbation of the priorities (0: none)[, its amplitude, 1e-3 by
+    default]) -- the schedule is a heuristic, and these pick among equally valid
+    ones."""
     leaf = LEAF
     jac_roots = [x for _, x in sorted(out["jac"].items())] if jac else []
     roots = list(out["rhs"]) + jac_roots
@@ -523,14 +525,14 @@ def schedule(P: Program, out: dict, G: int, jac: bool, limit=None, first_scratch
             if pend[u] == 0:
                 order.append(u)
     assert len(order) == len(comp), "the program has a cycle"
-    lat_t, hold, seed = tune or (LATENCY[C_EXP], None, 0)
+    lat_t, hold, seed, amp = (tuple(tune) + (1e-3,))[:4] if tune else (LATENCY[C_EXP], None, 0, 0.0)
     lat = dict(LATENCY)
     lat.update({C_EXP: lat_t, C_LOG: lat_t, C_SQRT: max(1.0, lat_t - 1.0)})
     rng = random.Random(seed)
     prio = {}
     for x in reversed(order):
         prio[x] = lat[kind(x)] + max((prio[u] for u in users[x]), default=0.0)
-        prio[x] += rng.random() * 1e-3 if seed else 0.0
+        prio[x] += rng.random() * amp if seed else 0.0
     steps = sink_riders(list_schedule(comp, cargs, users, kind, prio, G, limit, hold), users, kind, G)
     done_at = {}
     for s, (cls, take, riders) in enumerate(steps):
