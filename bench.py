@@ -33,8 +33,9 @@ batching form (``--forms-batch-scale``).
 
 ``--impl reference`` times the reference's CPU path (the same CPU oracle) instead:
 each step is a 16^3 full collapse on all host cores.  Other modes: ``--diff``,
-``--batch``, ``--probe-fp64``, and the profiling drivers ``--profile-steps`` and
-``--profile-policy``.
+``--batch``, ``--probe-fp64``, the profiling drivers ``--profile-steps`` and
+``--profile-policy``, and ``--profile-phases`` (the cooperative advance's phase
+counters over one collapse).
 
 Multi-GPU: the path does not shard (every outer step needs the grid-wide minimum
 over all cells); N > 1 runs N independent replicas, one per GPU.
@@ -688,6 +689,38 @@ def profile_policy(args):
     return 0 if rc == wr.SUCCESS else 1
 
 
+def profile_phases(args):
+    """--profile-phases: one full collapse of the grid through wr_run with the
+    cooperative advance's phase counters on (wr_diag_coop_phases): cycles per
+    phase of an attempt of one warp, and each phase's share."""
+    import warp_reactor_gb300 as wr
+    from warp_reactor_gb300 import build
+    build.build_all()
+    cells = wr.make_grid(args.grid)
+    math_mode = wr.MATH_CUDA if args.math == "cuda" else wr.MATH_PORTABLE
+    with wr.Context(len(cells), 0, math_mode) as ctx:
+        if args.variant is not None:
+            ctx.set_variant(args.variant)
+        ctx.phase_counters(True)
+        ctx.set_profiling(True)
+        ctx.upload(cells)
+        rc, cgs = ctx.run(True)
+        t = ctx.run_timing()
+        ph = ctx.read_phases()
+        ctx.download(cells)
+    names = wr.Context.PHASES
+    total = sum(ph[k] for k in names)
+    print(json.dumps({
+        "mode": "profile-phases", "grid": args.grid, "math": args.math, "result": int(rc), "outer_steps": cgs,
+        "run_s_with_counters": t.run_ms / 1e3, "warps": ph["warps"], "warp_attempts": ph["attempts"],
+        "cycles_per_warp_attempt": {k: ph[k] / max(ph["attempts"], 1) for k in names},
+        "share": {k: ph[k] / max(total, 1) for k in names},
+        "phase_cycles_over_warp_cycles": total / max(ph["cycles"], 1),
+        "cell_attempts": int(cells["stats"]["internal_steps"].sum()),
+    }), flush=True)
+    return 0 if rc == wr.SUCCESS else 1
+
+
 def profile_steps(args):
     """A short, fixed run for ncu: ``--profile-steps S`` outer steps of the grid
     through wr_prepare / wr_advance (the same kernels as wr_run)."""
@@ -744,6 +777,8 @@ def main():
                     help="profiling driver: one full collapse with this policy through wr_run, print nothing, exit")
     ap.add_argument("--variant", type=int, default=None,
                     help="advance launch shape of --profile-steps (wr_set_advance_variant; default: the library's)")
+    ap.add_argument("--profile-phases", action="store_true",
+                    help="diagnostic: one full collapse with the cooperative advance's phase counters, print them, exit")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiling driver: run this many outer steps host-stepped, print nothing, exit")
     args = ap.parse_args()
@@ -755,6 +790,8 @@ def main():
         return batch_form(args)
     if args.profile_policy:
         return profile_policy(args)
+    if args.profile_phases:
+        return profile_phases(args)
     if args.profile_steps > 0:
         return profile_steps(args)
     if args.warmup < 3:

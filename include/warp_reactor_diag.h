@@ -75,6 +75,25 @@ int wr_diag_fp64_issue(int warps, int chains, double* cycles_per_instr);
  * denominator of the reference's FP64-bound path, measured on the same device. */
 int wr_diag_fp64_peak(double* dfma_per_s);
 
+/* Phase counters of the cooperative advance.  No reference counterpart: a
+ * diagnostic of where an attempt's time goes.  With on != 0 the context's
+ * cooperative advance launches (wr_advance, wr_run) run an instrumented
+ * instantiation of the kernel that adds, per warp, the clock64 cycles of each
+ * phase of its ROS2S attempts into 16 device counters (allocated here, zeroed):
+ *   [0] work queue, prologue and epilogue   [1] Jacobian+RHS program
+ *   [2] output loads, Jacobian gather, diagonal, stage combinations
+ *   [3] LU and the pivots' reciprocals      [4] stage solves
+ *   [5] RHS programs                        [6] error norm and step-size control
+ *   [7] attempts (per warp: two cells at 16 lanes per cell)
+ *   [8] cycles from a warp's start to its exit   [9] warps
+ * Results are unchanged; the counters cost a few percent of speed.  on = 0
+ * frees them and returns to the plain kernel. */
+int wr_diag_coop_phases(wr_ctx* ctx, int on);
+
+/* Copy the 16 phase counters to out16 (host) and, with reset != 0, zero them.
+ * Fails when the counters are off. */
+int wr_diag_coop_phases_read(wr_ctx* ctx, unsigned long long* out16, int reset);
+
 #ifdef __cplusplus
 }
 #endif

@@ -286,6 +286,32 @@ def test_advance_variants_identical(wr, gpu, variant):
     assert a.tobytes() == b.tobytes()
 
 
+@pytest.mark.parametrize("variant", [5, 6, 7])
+def test_phase_counters_keep_results(wr, gpu, variant):
+    """The cooperative advance with its phase counters on (the instrumented
+    instantiation, inside the captured graph of wr_run) gives the same bits as
+    without; the counters cover every phase and count the attempts."""
+    a = wr.make_grid(3)
+    rc0, cgs0 = wr.run_cells(a, True)
+    b = wr.make_grid(3)
+    with wr.Context(len(b)) as ctx:
+        ctx.set_variant(variant)
+        ctx.phase_counters(True)
+        ctx.upload(b)
+        rc, cgs = ctx.run(True)
+        ph = ctx.read_phases(reset=True)
+        again = ctx.read_phases()
+        ctx.download(b)
+        ctx.phase_counters(False)
+    assert rc == rc0 == wr.SUCCESS and cgs == cgs0
+    assert a.tobytes() == b.tobytes()
+    phases = [ph[k] for k in wr.Context.PHASES]
+    assert all(v > 0 for v in phases[1:]), ph
+    assert sum(phases) <= ph["cycles"]
+    assert 0 < ph["attempts"] <= int(b["stats"]["internal_steps"].sum())
+    assert ph["warps"] > 0 and all(v == 0 for v in again.values())
+
+
 def test_precision_form_against_its_oracle(wr, gpu, oracle_prec, oracle_port):
     """The precision form (advance variant 3: FP32 factorisation in error-weighted
     variables + one FP64 residual sweep per stage solve) equals its own oracle

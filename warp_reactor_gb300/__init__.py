@@ -108,6 +108,8 @@ def lib() -> ctypes.CDLL:
         L.wr_get_run_timing.argtypes = [vp, ctypes.POINTER(RunTiming)]
         L.wr_dt_history.argtypes = [vp, vp, ctypes.c_int]
         L.wr_diag_fp64_peak.argtypes = [dp]
+        L.wr_diag_coop_phases.argtypes = [vp, ctypes.c_int]
+        L.wr_diag_coop_phases_read.argtypes = [vp, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int]
         L.wr_last_error.restype = ctypes.c_char_p
         L.wr_kernel_launch_count.restype = ctypes.c_uint64
         _lib = L
@@ -228,6 +230,26 @@ class Context:
         rc = lib().wr_set_profiling(self.handle, int(bool(on)))
         if rc != SUCCESS:
             raise WarpReactorError(rc, f"wr_set_profiling ({last_error()})")
+
+    PHASES = ("queue_prologue_epilogue", "jacobian_rhs_program", "loads_gather_combinations", "lu", "stage_solves",
+              "rhs_programs", "error_norm_controller")
+
+    def phase_counters(self, on: bool = True) -> None:
+        """Phase counters of the cooperative advance (wr_diag_coop_phases)."""
+        rc = lib().wr_diag_coop_phases(self.handle, int(bool(on)))
+        if rc != SUCCESS:
+            raise WarpReactorError(rc, f"wr_diag_coop_phases ({last_error()})")
+
+    def read_phases(self, reset: bool = False) -> dict:
+        """The phase counters: cycles per phase (summed over warps), attempts,
+        total cycles and warps (wr_diag_coop_phases_read)."""
+        buf = (ctypes.c_ulonglong * 16)()
+        rc = lib().wr_diag_coop_phases_read(self.handle, buf, int(bool(reset)))
+        if rc != SUCCESS:
+            raise WarpReactorError(rc, f"wr_diag_coop_phases_read ({last_error()})")
+        out = {name: int(buf[k]) for k, name in enumerate(self.PHASES)}
+        out.update({"attempts": int(buf[7]), "cycles": int(buf[8]), "warps": int(buf[9])})
+        return out
 
     def run_timing(self) -> RunTiming:
         t = RunTiming()

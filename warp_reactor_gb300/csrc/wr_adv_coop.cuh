@@ -40,19 +40,32 @@ static_assert(kSmem <= 232448, "cooperative advance: shared memory of one block 
 }  // namespace
 
 cudaError_t WR_CAT(configure_advance_coop, WR_COOP_G)() {
-    cudaError_t e = cudaFuncSetAttribute(k_advance_coop<PortableMathCall, kG, kW, Tab>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kSmem));
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_advance_coop<CudaMath, kG, kW, Tab>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                static_cast<int>(kSmem));
+    const void* kernels[4] = {reinterpret_cast<const void*>(k_advance_coop<PortableMathCall, kG, kW, Tab, false>),
+                              reinterpret_cast<const void*>(k_advance_coop<CudaMath, kG, kW, Tab, false>),
+                              reinterpret_cast<const void*>(k_advance_coop<PortableMathCall, kG, kW, Tab, true>),
+                              reinterpret_cast<const void*>(k_advance_coop<CudaMath, kG, kW, Tab, true>)};
+    for (const void* k : kernels) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kSmem));
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
+// phases: the 16 phase counters of the instrumented instantiation (nullptr: the
+// plain kernel)
 cudaError_t WR_CAT(launch_advance_coop, WR_COOP_G)(int math_cuda, int blocks, cudaStream_t stream, DevState s,
-                                                   StepCtl* ctl) {
-    if (math_cuda)
-        k_advance_coop<CudaMath, kG, kW, Tab><<<blocks, kW * 32, kSmem, stream>>>(s, ctl);
-    else
-        k_advance_coop<PortableMathCall, kG, kW, Tab><<<blocks, kW * 32, kSmem, stream>>>(s, ctl);
+                                                   StepCtl* ctl, unsigned long long* phases) {
+    if (phases) {
+        if (math_cuda)
+            k_advance_coop<CudaMath, kG, kW, Tab, true><<<blocks, kW * 32, kSmem, stream>>>(s, ctl, phases);
+        else
+            k_advance_coop<PortableMathCall, kG, kW, Tab, true><<<blocks, kW * 32, kSmem, stream>>>(s, ctl, phases);
+    } else if (math_cuda) {
+        k_advance_coop<CudaMath, kG, kW, Tab, false><<<blocks, kW * 32, kSmem, stream>>>(s, ctl, nullptr);
+    } else {
+        k_advance_coop<PortableMathCall, kG, kW, Tab, false><<<blocks, kW * 32, kSmem, stream>>>(s, ctl, nullptr);
+    }
     return cudaGetLastError();
 }
 

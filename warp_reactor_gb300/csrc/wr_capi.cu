@@ -69,6 +69,8 @@ struct wr_ctx {
     int graph_variant = -1;
     int graph_policy = -1;
     int graph_timed = -1;  // the captured graph records the per-kernel events
+    int graph_phases = -1; // the captured graph launches the phase-counting advance
+    unsigned long long* phases = nullptr;  // wr_diag_coop_phases: 16 device counters
     int policy = WR_POLICY_GRIDWIDE_INDEPENDENT;
     double* local_dt = nullptr;  // legacy-local policy: each cell's own dt
     double* cta_j = nullptr;     // cta32 policy: per-cell Jacobian [225][n]
@@ -353,9 +355,9 @@ cudaError_t launch_advance(wr_ctx* ctx) {
     if (is_coop(ctx->variant)) {
         const int math_cuda = ctx->math == WR_MATH_CUDA ? 1 : 0;
         switch (kAdvanceShapes[ctx->variant].coop_lanes) {
-            case 8: return launch_advance_coop8(math_cuda, blocks, ctx->stream, ctx->s, ctx->ctl);
-            case 32: return launch_advance_coop32(math_cuda, blocks, ctx->stream, ctx->s, ctx->ctl);
-            default: return launch_advance_coop16(math_cuda, blocks, ctx->stream, ctx->s, ctx->ctl);
+            case 8: return launch_advance_coop8(math_cuda, blocks, ctx->stream, ctx->s, ctx->ctl, ctx->phases);
+            case 32: return launch_advance_coop32(math_cuda, blocks, ctx->stream, ctx->s, ctx->ctl, ctx->phases);
+            default: return launch_advance_coop16(math_cuda, blocks, ctx->stream, ctx->s, ctx->ctl, ctx->phases);
         }
     }
     if (ctx->math == WR_MATH_CUDA)
@@ -542,6 +544,7 @@ void wr_destroy(wr_ctx* ctx) {
     cudaFree(ctx->cta_e);
     cudaFree(ctx->dt_hist);
     cudaFree(ctx->staging);
+    cudaFree(ctx->phases);
     cudaFreeHost(ctx->host_ctl);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -645,7 +648,7 @@ static cudaError_t launch_step(wr_ctx* ctx, int slot) {
 
 static int ensure_graph(wr_ctx* ctx) {
     if (ctx->graph && ctx->graph_variant == ctx->variant && ctx->graph_policy == ctx->policy &&
-        ctx->graph_timed == (ctx->profiling ? 1 : 0))
+        ctx->graph_timed == (ctx->profiling ? 1 : 0) && ctx->graph_phases == (ctx->phases ? 1 : 0))
         return WR_SUCCESS;
     if (ctx->graph) {
         cudaGraphExecDestroy(ctx->graph);
@@ -668,6 +671,7 @@ static int ensure_graph(wr_ctx* ctx) {
     ctx->graph_variant = ctx->variant;
     ctx->graph_policy = ctx->policy;
     ctx->graph_timed = ctx->profiling ? 1 : 0;
+    ctx->graph_phases = ctx->phases ? 1 : 0;
     return WR_SUCCESS;
 }
 
@@ -907,6 +911,37 @@ int wr_set_profiling(wr_ctx* ctx, int on) {
         }
     }
     ctx->profiling = on != 0;
+    return WR_SUCCESS;
+}
+
+int wr_diag_coop_phases(wr_ctx* ctx, int on) {
+    if (!ctx) return fail_msg("wr_diag_coop_phases: null context");
+    int rc = set_device(ctx);
+    if (rc != WR_SUCCESS) return rc;
+    if (on && !ctx->phases) {
+        cudaError_t e = cudaMalloc(&ctx->phases, 16 * sizeof(unsigned long long));
+        if (e == cudaSuccess) e = cudaMemset(ctx->phases, 0, 16 * sizeof(unsigned long long));
+        if (e != cudaSuccess) return fail("wr_diag_coop_phases", e);
+    }
+    if (!on && ctx->phases) {
+        const cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        cudaFree(ctx->phases);
+        ctx->phases = nullptr;
+        if (e != cudaSuccess) return fail("wr_diag_coop_phases", e);
+    }
+    return WR_SUCCESS;
+}
+
+int wr_diag_coop_phases_read(wr_ctx* ctx, unsigned long long* out16, int reset) {
+    if (!ctx || !out16) return fail_msg("wr_diag_coop_phases_read: null argument");
+    if (!ctx->phases) return fail_msg("wr_diag_coop_phases_read: phase counters are off (wr_diag_coop_phases)");
+    int rc = set_device(ctx);
+    if (rc != WR_SUCCESS) return rc;
+    cudaError_t e = cudaMemcpyAsync(out16, ctx->phases, 16 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                    ctx->stream);
+    if (e == cudaSuccess && reset) e = cudaMemsetAsync(ctx->phases, 0, 16 * sizeof(unsigned long long), ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return fail("wr_diag_coop_phases_read", e);
     return WR_SUCCESS;
 }
 

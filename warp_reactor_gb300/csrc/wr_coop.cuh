@@ -399,10 +399,54 @@ __device__ __forceinline__ void gather_matrix(uint64_t* V, const uint16_t* jac, 
 
 }  // namespace coop
 
+// Phase counters (a diagnostic, wr_diag_coop_phases): the instrumented
+// instantiation adds, per warp, the clock64 cycles of each phase of its attempts
+// into 16 device counters: [0] queue, prologue and epilogue, [1] Jacobian+RHS
+// program, [2] output loads, Jacobian gather, diagonal and stage combinations,
+// [3] LU, [4] stage solves, [5] RHS programs, [6] error norm and controller,
+// [7] attempts, [8] cycles from start to exit, [9] warps.  The plain
+// instantiation compiles every call to nothing.
+enum { PH_QUEUE = 0, PH_JPROG = 1, PH_MISC = 2, PH_LU = 3, PH_SOLVE = 4, PH_RPROG = 5, PH_CTL = 6 };
+__device__ __forceinline__ long long phase_now() {
+#if defined(__CUDA_ARCH__)
+    return clock64();
+#else
+    return 0;
+#endif
+}
+template <bool ON>
+struct PhaseClock {
+    __device__ __forceinline__ void mark(int) {}
+    __device__ __forceinline__ void attempt() {}
+    __device__ __forceinline__ void flush(unsigned long long*, int) {}
+};
+template <>
+struct PhaseClock<true> {
+    long long acc[7] = {0, 0, 0, 0, 0, 0, 0};
+    long long t0, t, attempts = 0;
+    __device__ __forceinline__ PhaseClock() : t0(phase_now()), t(t0) {}
+    __device__ __forceinline__ void mark(int k) {
+        const long long now = phase_now();
+        acc[k] += now - t;
+        t = now;
+    }
+    __device__ __forceinline__ void attempt() { ++attempts; }
+    __device__ __forceinline__ void flush(unsigned long long* out, int lane) {
+        mark(PH_QUEUE);
+        if (lane != 0 || out == nullptr) return;
+#pragma unroll
+        for (int k = 0; k < 7; ++k) atomicAdd(out + k, static_cast<unsigned long long>(acc[k]));
+        atomicAdd(out + 7, static_cast<unsigned long long>(attempts));
+        atomicAdd(out + 8, static_cast<unsigned long long>(phase_now() - t0));
+        atomicAdd(out + 9, 1ULL);
+    }
+};
+
 // The cooperative burn: persistent blocks of W warps, G lanes per cell, each group
-// taking cells from the work queue until it is empty.
-template <class M, int G, int W, class Tab>
-__global__ void __launch_bounds__(W * 32, 1) k_advance_coop(DevState s, StepCtl* ctl) {
+// taking cells from the work queue until it is empty.  PH: the phase-counting
+// instantiation (phases: its 16 counters).
+template <class M, int G, int W, class Tab, bool PH = false>
+__global__ void __launch_bounds__(W * 32, 1) k_advance_coop(DevState s, StepCtl* ctl, unsigned long long* phases) {
     using namespace coop;
     constexpr int K = (NEQ + G - 1) / G;
     constexpr int SLOTS = 32 / G;
@@ -418,6 +462,7 @@ __global__ void __launch_bounds__(W * 32, 1) k_advance_coop(DevState s, StepCtl*
     const int n = s.n;
     const unsigned int queued = ctl->queued;
 
+    PhaseClock<PH> pc;
     Lane L;
     int cell = -1, g = 0;
     bool have = false;
@@ -504,11 +549,14 @@ __global__ void __launch_bounds__(W * 32, 1) k_advance_coop(DevState s, StepCtl*
             break;
         }
         if (exhausted) break;
+        pc.mark(PH_QUEUE);
+        pc.attempt();
 
         // ---- one ROS2S attempt, reproducer.cpp:7259-7345
         store_inputs<G, K>(V, y, gl);
         __syncwarp(gmask);
         run_prog<M, G>(Tab::jprog(), Tab::jlit(), Tab::kJSteps, gl, V, gmask);
+        pc.mark(PH_JPROG);
         load_outputs<G, K>(V, Tab::jout(), f0, gl);
         gather_matrix<G>(V, Tab::jac(), gl, gmask);
         if (L.fresh) L.n_jac += 1;
@@ -521,6 +569,7 @@ __global__ void __launch_bounds__(W * 32, 1) k_advance_coop(DevState s, StepCtl*
             if (c < NEQ) E[c * NEQ + c] = E[c * NEQ + c] + fac;
         }
         __syncwarp(gmask);
+        pc.mark(PH_MISC);
         const int info = lu_coop<G>(E, gl, gmask, ip);
         if (info != 0) {
             L.nsing += 1;
@@ -548,9 +597,11 @@ __global__ void __launch_bounds__(W * 32, 1) k_advance_coop(DevState s, StepCtl*
         L.n_decomp += 1;
         uint64_t rY[K];
         diag_recips<G, K>(E, rY, gl);
+        pc.mark(PH_LU);
 #pragma unroll
         for (int t = 0; t < K; ++t) ak1[t] = f0[t];
         solve_coop<G, K>(E, ip, rY, ak1, gl, gmask);
+        pc.mark(PH_SOLVE);
         // stage 2
         {
             double yn[K];
@@ -562,12 +613,16 @@ __global__ void __launch_bounds__(W * 32, 1) k_advance_coop(DevState s, StepCtl*
             }
             store_inputs<G, K>(V, yn, gl);
             __syncwarp(gmask);
+            pc.mark(PH_MISC);
             run_prog<M, G>(Tab::rprog(), Tab::rlit(), Tab::kRSteps, gl, V, gmask);
+            pc.mark(PH_RPROG);
             double dy[K];
             load_outputs<G, K>(V, Tab::rout(), dy, gl);
 #pragma unroll
             for (int t = 0; t < K; ++t) w[t] += dy[t];
+            pc.mark(PH_MISC);
             solve_coop<G, K>(E, ip, rY, w, gl, gmask);
+            pc.mark(PH_SOLVE);
 #pragma unroll
             for (int t = 0; t < K; ++t) ak2[t] = w[t];
         }
@@ -582,12 +637,16 @@ __global__ void __launch_bounds__(W * 32, 1) k_advance_coop(DevState s, StepCtl*
             __syncwarp(gmask);  // every lane has read the stage-2 outputs
             store_inputs<G, K>(V, yn, gl);
             __syncwarp(gmask);
+            pc.mark(PH_MISC);
             run_prog<M, G>(Tab::rprog(), Tab::rlit(), Tab::kRSteps, gl, V, gmask);
+            pc.mark(PH_RPROG);
             double dy[K];
             load_outputs<G, K>(V, Tab::rout(), dy, gl);
 #pragma unroll
             for (int t = 0; t < K; ++t) w[t] += dy[t];
+            pc.mark(PH_MISC);
             solve_coop<G, K>(E, ip, rY, w, gl, gmask);
+            pc.mark(PH_SOLVE);
         }
         // w = k3: candidate and error estimate, reproducer.cpp:7299-7304
         double ynew[K], sq[K];
@@ -655,7 +714,9 @@ __global__ void __launch_bounds__(W * 32, 1) k_advance_coop(DevState s, StepCtl*
             }
         }
         __syncwarp(gmask);  // the next attempt overwrites V: every lane is done with it
+        pc.mark(PH_CTL);
     }
+    pc.flush(phases, lane);
 }
 
 // ---------------------------------------------------------------- diagnostics

@@ -61,9 +61,12 @@ cudaError_t configure_advance_cuda();
 cudaError_t configure_advance_coop8();
 cudaError_t configure_advance_coop16();
 cudaError_t configure_advance_coop32();
-cudaError_t launch_advance_coop8(int math_cuda, int blocks, cudaStream_t stream, DevState s, StepCtl* ctl);
-cudaError_t launch_advance_coop16(int math_cuda, int blocks, cudaStream_t stream, DevState s, StepCtl* ctl);
-cudaError_t launch_advance_coop32(int math_cuda, int blocks, cudaStream_t stream, DevState s, StepCtl* ctl);
+cudaError_t launch_advance_coop8(int math_cuda, int blocks, cudaStream_t stream, DevState s, StepCtl* ctl,
+                                  unsigned long long* phases);
+cudaError_t launch_advance_coop16(int math_cuda, int blocks, cudaStream_t stream, DevState s, StepCtl* ctl,
+                                  unsigned long long* phases);
+cudaError_t launch_advance_coop32(int math_cuda, int blocks, cudaStream_t stream, DevState s, StepCtl* ctl,
+                                  unsigned long long* phases);
 // diagnostics of the cooperative programs and LU on device buffers (wr_diag.cu)
 cudaError_t diag_coop_network8(int math_cuda, int n, const double* y, double* J, double* f, double* f2);
 cudaError_t diag_coop_network16(int math_cuda, int n, const double* y, double* J, double* f, double* f2);
