@@ -60,10 +60,10 @@ def _stale(target: str, deps) -> bool:
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
-def _run(cmd, verbose=False):
+def _run(cmd, verbose=False, env=None):
     if verbose:
         print(" ".join(cmd), flush=True)
-    r = subprocess.run(cmd, capture_output=True, text=True)
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env)
     if r.returncode != 0:
         raise RuntimeError(f"command failed ({r.returncode}): {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     return r.stdout + r.stderr
@@ -173,8 +173,16 @@ def build_reference_oracle(verbose=False) -> None:
     if not (os.path.exists(ref_src) and os.path.exists(script)):
         return
     deps = [ref_src, script, os.path.join(ORACLE, "ref_shim.cpp"), os.path.join(INCLUDE, "warp_reactor.h")]
-    if _stale(os.path.join(ORACLE, "_ref", "libwr_ref.so"), deps):
-        _run(["sh", script], verbose)
+    cuda_deps = [ref_src, script, os.path.join(ORACLE, "ref_cuda_shim.cu")]
+    # The reference's CUDA kernels (plain and structured) are device code: built
+    # here, they travel with the repository to a GPU host that has no reference tree.
+    env = dict(os.environ, WITH_CUBIN="1", WITH_STRUCTURED="1", PATH=os.path.dirname(_nvcc()) + os.pathsep +
+               os.environ.get("PATH", ""))
+    stale = _stale(os.path.join(ORACLE, "_ref", "libwr_ref.so"), deps)
+    for name in ("ref_kernels.cubin", "ref_structured.cubin"):
+        stale = stale or _stale(os.path.join(ORACLE, "_ref", name), cuda_deps)
+    if stale:
+        _run(["sh", script], verbose, env=env)
 
 
 def build_all(verbose=False) -> dict:
