@@ -777,6 +777,40 @@ def generate(G: int, dag=None, limit="default", tune="default"):
     return {"G": G, "nv": nv, "rconst": rconst, "rfun": rfun, "progs": progs, "warps": warps_per_block(G, nv)}
 
 
+def shared_wavefronts(pr: dict) -> dict:
+    """Shared-memory wavefronts of one encoded program's slot accesses, per half
+    warp, by operand (X, Y, Z, D of the main word; A, B, C, D2 of the integer word),
+    against one wavefront per access.  A 64-bit access of a half warp (one cell's
+    G = 16 lanes) is conflict-free when its distinct slots lie in distinct bank
+    pairs (slot mod 16: the cell's array base is uniform over the half warp);
+    otherwise it takes as many wavefronts as the most-used bank pair holds distinct
+    slots.  Accesses follow the interpreter: an FMA step loads X, Y, Z; exp, log
+    and sqrt load Y, division X and Y; every non-idle step stores D; a step with
+    integer nodes loads A, B, C and stores D2."""
+    def wf(slots):
+        by = collections.defaultdict(set)
+        for s in slots:
+            by[s % 16].add(s)
+        return max(len(v) for v in by.values())
+
+    def field(w, k):
+        return ((w >> (16 * k)) & 0xffff) >> 3
+
+    got, ideal = collections.Counter(), collections.Counter()
+    for lanes in pr["words"][:pr["nsteps"]]:
+        m0 = lanes[0][0]
+        cls, flint = (m0 >> 48) & 7, (m0 >> 32) & FL_INT
+        used = {C_FMA: "XYZD", C_DIV: "XYD"}.get(cls, "YD" if cls != C_NONE else "")
+        acc = [(n, [field(m, "XYZD".index(n)) for m, _, _ in lanes]) for n in used]
+        if flint:
+            acc += [(n, [field(i, k) for _, i, _ in lanes]) for k, n in enumerate(("A", "B", "C", "D2"))]
+        for n, slots in acc:
+            got[n] += wf(slots)
+            ideal[n] += 1
+    return {"wavefronts": sum(got.values()), "ideal": sum(ideal.values()),
+            "by_operand": {n: (got[n], ideal[n]) for n in sorted(got)}}
+
+
 def stats(sch: Schedule) -> dict:
     cnt = collections.Counter(c for c, _, _ in sch.steps)
     cost = sum(STEP_COST.get(c, 0.0) for c, _, _ in sch.steps)
@@ -859,3 +893,7 @@ if __name__ == "__main__":
     for G in LANES_PER_CELL:
         g = generate(G, d)
         print(G, g["nv"], len(g["rconst"]), g["warps"], {k: v["stats"] for k, v in g["progs"].items()})
+        if G == 16:
+            print("  shared wavefronts per half warp:",
+                  {k: {f: w[f] for f in ("wavefronts", "ideal")} for k, w in
+                   ((k, shared_wavefronts(v)) for k, v in g["progs"].items())})
