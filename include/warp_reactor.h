@@ -185,7 +185,7 @@ int wr_set_profiling(wr_ctx* ctx, int on);
  *      FP32 with one FP64-residual refinement sweep per stage solve; RHS,
  *      exp/log, stage combination, error norm, controller and EOS stay FP64
  *   4  one lane per cell, 384 lanes per SM (1 block), matrix in global memory
- *   5  cooperative: 8 lanes per cell (4 cells per warp), 10 warps per SM
+ *   5  cooperative: 8 lanes per cell (4 cells per warp), 9 warps per SM
  *   6  cooperative: 16 lanes per cell (2 cells per warp), 16 warps per SM (default)
  *   7  cooperative: 32 lanes per cell (1 cell per warp), 16 warps per SM
  * The cooperative advance evaluates one cell's network, LU factorisation and
