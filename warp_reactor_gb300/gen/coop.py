@@ -488,7 +488,8 @@ def sink_riders(steps, users, kind, G):
     return [(cls, take, lanes[s]) for s, (cls, take, _) in enumerate(steps) if take or lanes[s]]
 
 
-def schedule(P: Program, out: dict, G: int, jac: bool, limit=None, first_scratch=RES_BASE, tune=None):
+def schedule(P: Program, out: dict, G: int, jac: bool, limit=None, first_scratch=RES_BASE, tune=None,
+             banked=None):
     """List-schedule the program into steps of width G and allocate slots.
 
     ``jac``: the program computes the Jacobian too.  Its 225 entries are kept
@@ -501,7 +502,9 @@ def schedule(P: Program, out: dict, G: int, jac: bool, limit=None, first_scratch
     (latency weight of exp/log/sqrt, ``hold`` of the list scheduler, seed of a
     random perturbation of the priorities (0: none)[, its amplitude, 1e-3 by
     default]) -- the schedule is a heuristic, and these pick among equally valid
-    ones."""
+    ones.  ``banked``: (reserved slot map, slot cap) to allocate slots with
+    ``allocate_banked`` (G = 16), falling back to the linear scan when it finds
+    no room below the cap."""
     leaf = LEAF
     jac_roots = [x for _, x in sorted(out["jac"].items())] if jac else []
     roots = list(out["rhs"]) + jac_roots
@@ -551,8 +554,16 @@ def schedule(P: Program, out: dict, G: int, jac: bool, limit=None, first_scratch
                 if P.nodes[a][0] == "in" or P.nodes[a][0] not in leaf:
                     last[a] = s
     keep = {resolve(P, r)[0] for r in roots}
-    slot = {}
     inputs = [x for x in range(len(P.nodes)) if P.nodes[x][0] == "in"]
+    if banked is not None and G == BANKS:
+        got = allocate_banked(P, steps, last, keep, inputs, banked[0], jac, first_scratch, banked[1] - 1)
+        if got is not None:
+            slot, nv = got
+            outputs = {"rhs": [resolve(P, r) for r in out["rhs"]]}
+            if jac:
+                outputs["jac"] = [resolve(P, x) for x in jac_roots]
+            return Schedule(G, steps, slot, nv + 1, outputs, None), args  # + the write sink
+    slot = {}
     low = list(range(E_SLOTS)) if jac else []  # min-heaps of free slots
     high = []
     next_slot = first_scratch
@@ -588,6 +599,221 @@ def schedule(P: Program, out: dict, G: int, jac: bool, limit=None, first_scratch
     if jac:
         outputs["jac"] = [resolve(P, x) for x in jac_roots]
     return Schedule(G, steps, slot, nv, outputs, None), args
+
+
+def operand_refs(P: Program, x: int, res: dict) -> dict:
+    """The operands the interpreter loads for node x, by field (X, Y, Z of a main
+    node; A, B, C of an integer node), as ``encode`` lays them out: ``("n", node)``
+    for a computed value, ``("s", slot)`` for a fixed slot (an input, a reserved
+    constant, a transcendental of a constant).  A constant that rides as the
+    lane's literal loads the +0.0 slot."""
+    ZERO, IONE, ONE, MONE, MZERO = (("s", res[b]) for b in (0, 1, dbits(1.0), dbits(-1.0), dbits(-0.0)))
+
+    def const(y):
+        return P.nodes[resolve(P, y)[0]][0] == "const"
+
+    def ref(y):
+        b = resolve(P, y)[0]
+        op, a = P.nodes[b]
+        if op == "const":
+            return ("s", res[a[0]])
+        if op == "dconst":
+            return ("s", res[a])
+        if op == "in":
+            return ("s", Y_BASE + a[0])
+        return ("n", b)
+
+    op, a = P.nodes[x]
+    if op == "mul":
+        if const(a[0]) or const(a[1]):
+            return {"X": ref(a[1] if const(a[0]) else a[0]), "Y": ZERO, "Z": MZERO}
+        return {"X": ref(a[0]), "Y": ref(a[1]), "Z": MZERO}
+    if op == "add":
+        if const(a[0]) or const(a[1]):
+            return {"X": ONE, "Y": ZERO, "Z": ref(a[1] if const(a[0]) else a[0])}
+        return {"X": ref(a[0]), "Y": ONE, "Z": ref(a[1])}
+    if op == "sub":
+        if const(a[1]):
+            return {"X": ONE, "Y": ZERO, "Z": ref(a[0])}
+        return {"X": ref(a[1]), "Y": MONE, "Z": ref(a[0])}
+    if op == "div":
+        if const(a[0]):
+            return {"X": ref(a[1]), "Y": ZERO}
+        if const(a[1]):
+            return {"X": ref(a[0]), "Y": ZERO}
+        return {"X": ref(a[0]), "Y": ref(a[1])}
+    if op in MAIN_CLASS:  # exp, log, sqrt
+        return {"Y": ZERO if const(a[0]) else ref(a[0])}
+    if op == "and":
+        return {"A": ref(a[0]), "B": ref(a[1]), "C": ZERO}
+    if op == "or":
+        return {"A": ref(a[0]), "B": IONE, "C": ref(a[1])}
+    if op == "not":
+        return {"A": ref(a[0]), "B": ZERO, "C": IONE}
+    if op == "sel":
+        return {"A": ref(a[0]), "B": ref(a[1]), "C": ref(a[2])}
+    if op in ("le", "lt"):
+        return {"A": ref(a[0]), "B": ref(a[1]), "C": ONE}
+    return {"A": ref(a[0]), "B": ONE, "C": ONE}  # sneg, sabs
+
+
+def _assign(cost) -> list:
+    """Minimum-cost assignment of n rows to distinct columns of an n x m cost
+    matrix (n <= m; Hungarian method with potentials): the column of each row."""
+    n, m = len(cost), len(cost[0])
+    INF = float("inf")
+    u, v = [0.0] * (n + 1), [0.0] * (m + 1)
+    p, way = [0] * (m + 1), [0] * (m + 1)
+    for i in range(1, n + 1):
+        p[0] = i
+        j0 = 0
+        minv = [INF] * (m + 1)
+        used = [False] * (m + 1)
+        while True:
+            used[j0] = True
+            i0, delta, j1 = p[j0], INF, 0
+            for j in range(1, m + 1):
+                if not used[j]:
+                    cur = cost[i0 - 1][j - 1] - u[i0] - v[j]
+                    if cur < minv[j]:
+                        minv[j], way[j] = cur, j0
+                    if minv[j] < delta:
+                        delta, j1 = minv[j], j
+            for j in range(m + 1):
+                if used[j]:
+                    u[p[j]] += delta
+                    v[j] -= delta
+                else:
+                    minv[j] -= delta
+            j0 = j1
+            if p[j0] == 0:
+                break
+        while j0:
+            j1 = way[j0]
+            p[j0] = p[j1]
+            j0 = j1
+    col = [0] * n
+    for j in range(1, m + 1):
+        if p[j]:
+            col[p[j] - 1] = j - 1
+    return col
+
+
+BANKS = 16  # bank pairs of a 64-bit shared access by one half warp
+# allocate_banked: cost per slot of a bank's planned occupancy within BANK_MARGIN
+# of its room (chosen with shared_wavefronts: 1 and 2.0 give the fewest)
+BANK_MARGIN = 1
+BANK_FILL = 2.0
+
+
+def allocate_banked(P: Program, steps, last, keep, inputs, res, jac: bool, first_scratch: int, cap: int):
+    """Slot allocation that spreads every shared access of a half warp (one cell's
+    16 lanes) over the 16 bank pairs (slot mod 16).
+
+    Each value's bank is chosen when its step is allocated, by a minimum-cost
+    assignment of the step's new values (main nodes, then integer nodes) to banks:
+    - a value costs one for every value already placed in that bank that is
+      loaded beside it (the same field of a step that reads both) and for every
+      fixed slot there (inputs, reserved constants);
+    - a second value of the step in one bank costs one (its store replays);
+    - the bank's planned occupancy over the value's lifetime (every placed value
+      is counted from its step to its last read) may not exceed the bank's slots
+      below ``cap``, and costs ``BANK_FILL`` per slot when it comes within
+      ``BANK_MARGIN`` of them: a bank that fills early would force conflicts (or
+      more slots) later.
+    Lifetimes are those of the linear scan: a slot read last in step s is free
+    from s + 1, so no step reads a slot that it also writes.  A value takes the
+    lowest free slot of its bank (the matrix slots first, for a Jacobian-program
+    value that is not kept), else the bank's next slot above ``first_scratch``.
+    Returns the slot map and the slot count, or None when a step finds no room."""
+    import heapq
+    groups, reads = [], collections.defaultdict(list)
+
+    def group(refs, idle):
+        fixed = [0] * BANKS
+        for r in set(refs) | ({idle} if idle else set()):
+            if r[0] == "s":
+                fixed[r[1] % BANKS] += 1
+            else:
+                reads[r[1]].append(len(groups))
+        groups.append(fixed)
+
+    ONE = ("s", res[dbits(1.0)])
+    for cls, take, riders in steps:
+        if cls != C_NONE:
+            maps = [operand_refs(P, x, res) for x in take]
+            for f in {C_FMA: "XYZ", C_DIV: "XY"}.get(cls, "Y"):
+                group([m[f] for m in maps], ONE if len(take) < BANKS else None)
+        if riders:
+            maps = [operand_refs(P, x, res) for x in riders]
+            short = len(riders) < BANKS
+            for f, idle in (("A", ("s", res[1])), ("B", ONE), ("C", ONE)):
+                group([m[f] for m in maps], idle if short else None)
+
+    S = len(steps)
+    end = {x: S + 1 if x in keep else last.get(x, s) for s, (_, take, riders) in enumerate(steps)
+           for x in take + riders}
+    room = [0] * BANKS  # slots of each bank: matrix (Jacobian program), inputs, scratch
+    for sl in [*range(E_SLOTS if jac else 0), *range(Y_BASE, RES_BASE), *range(first_scratch, cap)]:
+        room[sl % BANKS] += 1
+    occ = [[0] * (S + 2) for _ in range(BANKS)]
+    free = {"low": [[] for _ in range(BANKS)], "high": [[] for _ in range(BANKS)]}
+    if jac:
+        for sl in range(E_SLOTS):
+            heapq.heappush(free["low"][sl % BANKS], sl)
+    nxt = [first_scratch + ((b - first_scratch) % BANKS) for b in range(BANKS)]
+    slot = {}
+    release = collections.defaultdict(list)
+    for x in inputs:
+        slot[x] = sl = Y_BASE + P.nodes[x][1][0]
+        e = S + 1 if x in keep else last.get(x, -1)
+        for t in range(e + 1):
+            occ[sl % BANKS][t] += 1
+        if x in keep:
+            continue
+        if x in last:
+            release[last[x] + 1].append(sl)
+        else:
+            heapq.heappush(free["high"][sl % BANKS], sl)
+    top = first_scratch - 1
+    for s, (cls, take, riders) in enumerate(steps):
+        for sl in release.pop(s, []):
+            heapq.heappush(free["low" if sl < E_SLOTS else "high"][sl % BANKS], sl)
+        for nodes in (take, riders):
+            if not nodes:
+                continue
+            cost = []
+            for x in nodes:
+                pools = ("high",) if x in keep else ("low", "high")
+                row = []
+                for b in range(BANKS):
+                    peak = max(occ[b][s:end[x] + 1])
+                    if peak + 1 > room[b] or (nxt[b] >= cap and not any(free[p][b] for p in pools)):
+                        row.append(1e9)
+                        continue
+                    fill = max(0, peak + 1 - (room[b] - BANK_MARGIN))
+                    row.append(BANK_FILL * fill + sum(groups[g][b] for g in reads[x]))
+                cost.append(row + [c + 1.0 for c in row])
+            for x, col, row in zip(nodes, _assign(cost), cost):
+                if row[col] >= 1e9:
+                    return None
+                b = col % BANKS
+                pools = ("high",) if x in keep else ("low", "high")
+                pool = next((p for p in pools if free[p][b]), None)
+                if pool is not None:
+                    sl = heapq.heappop(free[pool][b])
+                else:
+                    sl = nxt[b]
+                    nxt[b] += BANKS
+                    top = max(top, sl)
+                slot[x] = sl
+                for t in range(s, end[x] + 1):
+                    occ[b][t] += 1
+                for g in reads[x]:
+                    groups[g][b] += 1
+                if x not in keep:
+                    release[last.get(x, s) + 1].append(sl)
+    return slot, max(top + 1, first_scratch)
 
 
 def encode(P: Program, sch: Schedule, res: dict) -> list:
@@ -712,6 +938,8 @@ SCHED_TUNE = {
 # in 32.5 s on GB300, 17 warps in 34.3 s and 19 warps (register-limited) in 33.3 s
 SMEM_BLOCK = 232448
 MAX_WARPS = 16
+# lane widths whose slots are allocated bank by bank (allocate_banked)
+BANKED = (16,)
 
 
 def warps_per_block(G: int, nv: int) -> int:
@@ -722,10 +950,11 @@ def warps_per_block(G: int, nv: int) -> int:
     return max(1, min(MAX_WARPS, cells // (32 // G)))
 
 
-def generate(G: int, dag=None, limit="default", tune="default"):
+def generate(G: int, dag=None, limit="default", tune="default", banked="default"):
     """Programs jrhs and rhs for G lanes per cell: a dict with the encoded steps,
     the output operands, the slot count, the reserved constants and the warps
-    per block."""
+    per block.  ``banked``: allocate slots with ``allocate_banked`` within the
+    slot count that keeps the block's warps (G = 16)."""
     dag = dag or ir_io.load()
     if limit == "default":
         limit = SCHED_LIMIT.get(G)
@@ -748,10 +977,16 @@ def generate(G: int, dag=None, limit="default", tune="default"):
     res = {b: RES_BASE + i for i, b in enumerate(rconst)}
     res.update({f: RES_BASE + len(rconst) + j for j, f in enumerate(rfun)})
     first = RES_BASE + len(rconst) + len(rfun)
+    if banked == "default":
+        banked = G in BANKED
+    # slot count (write sink included) that keeps the block's warps, one below the
+    # block's whole shared memory
+    cap = max(nv for nv in range(first, MAX_SLOTS) if warps_per_block(G, nv) == MAX_WARPS) - 1
     scheds = {}
     for kind, (P, out) in built.items():
         t, lim = (tune or {}).get(kind, (None, limit))
-        scheds[kind] = schedule(P, out, G, jac=(kind == "jrhs"), limit=lim, first_scratch=first, tune=t)
+        scheds[kind] = schedule(P, out, G, jac=(kind == "jrhs"), limit=lim, first_scratch=first, tune=t,
+                                banked=(res, cap) if banked else None)
     nv = max(sch.nv for sch, _ in scheds.values())
     if nv * 8 > 0xfff8:
         raise ValueError(f"{nv} slots do not fit the 16-bit byte offsets")
