@@ -72,7 +72,10 @@ program runs before the matrix is formed, so it uses the matrix slots as scratch
 too and keeps its results above them; the RHS program runs while the matrix holds
 the LU factors and never writes it.  Slots are allocated by a linear scan over
 the schedule, so the slot count is the largest live set, which sets the shared
-memory per cell and hence the cells (warps) per SM.
+memory per cell and hence the cells (warps) per SM.  At 16 lanes per cell (one
+cell per half warp) they are allocated bank by bank instead (``allocate_banked``),
+so that a step's loads and stores spread over the 16 bank pairs, within the slot
+count that keeps the block's warps.
 
 Scheduling is list scheduling by critical path (longest weighted path to an
 output) with one class per step; above a live-set limit, nodes whose operands die
