@@ -18,7 +18,9 @@ cells/s on H200, docs/performance/optimization-results.md:51).
           source-level operation counts, weighted exp/log = 25, sqrt/cbrt = 20,
           + - * / = 1, times the per-cell Jacobian and attempt counters) over its
           duration (event nodes inside the graph around every advance launch),
-          against this GPU's measured FP64 FMA rate
+          against this GPU's measured FP64 FMA rate; beside it the generated
+          programs' steps, FP64 issue slots and modelled shared-memory
+          wavefronts per attempt (programs_per_attempt)
   substeps  ROS2S attempts, accepted, rejected (exact: attempts - accepted) and
           Jacobians of the timed run, summed over cells
   cpu_baseline  the CPU oracle with C-library math (bitwise the reference's CPU
@@ -179,6 +181,26 @@ def algorithmic_ops(cells):
     cse = {"F_J_plus_RHS_cse": c["cse_jac_rhs_weighted"], "F_RHS_cse": c["cse_rhs_weighted"]}
     return nj * f_j + na * f_att, {"F_J": f_j, "F_RHS": f_rhs, "F_attempt": f_att, "jacobians": nj, "attempts": na,
                                    **cse}
+
+
+def program_figures(G=16):
+    """Figures of the default advance's generated vector programs (16 lanes per
+    cell, two cells per warp) per ROS2S attempt of one warp: steps and FP64 issue
+    slots of one Jacobian+RHS and two RHS programs, the slots per cell, and the
+    shared-memory wavefronts their slot accesses take per half warp against one
+    per access (coop.shared_wavefronts: the bank-conflict model)."""
+    from warp_reactor_gb300.gen import coop, ir_io
+    g = coop.generate(G, ir_io.load())
+    out = {"lanes_per_cell": G, "slots_per_cell": g["nv"], "warps_per_sm": g["warps"], "steps": 0,
+           "fp64_issue_slots": 0.0, "shared_wavefronts": 0, "shared_accesses": 0}
+    for kind, runs in (("jrhs", 1), ("rhs", 2)):
+        pr = g["progs"][kind]
+        w = coop.shared_wavefronts(pr)
+        out["steps"] += runs * pr["nsteps"]  # as executed: padded to a multiple of four
+        out["fp64_issue_slots"] += runs * pr["stats"]["fp64_slots"]
+        out["shared_wavefronts"] += runs * w["wavefronts"]
+        out["shared_accesses"] += runs * w["ideal"]
+    return out
 
 
 def precision_form(wr, device, math_mode, grid=16, steps=300):
@@ -620,7 +642,8 @@ def run_gb300(args, rank, ws, local, tdist):
                      "fp64_pipe_active_ncu": prof.get("fp64_pipe_active"),
                      "profile_source": prof.get("source"),
                      "kernel": "k_advance_coop", "launches": adv_launches,
-                     "ms_per_launch": adv_ms / max(adv_launches, 1), "algorithmic_ops_per_step": ops, **opinfo},
+                     "ms_per_launch": adv_ms / max(adv_launches, 1), "algorithmic_ops_per_step": ops, **opinfo,
+                     "programs_per_attempt": program_figures()},
         "cpu_baseline": cpu,
         "e2e": {"value": ws * n / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": n * 216,
                 "d2h_bytes_per_step": n * 216},
